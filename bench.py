@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Frames/s of the vkgs per-frame splat pipeline on GB300.
+
+Workload ("large"): 6,000,000 synthetic 3D Gaussians (70 % on a radius-4 shell, 30 % uniform in
+[-10,10]^3, seed 1), 1600x900, nine cameras (eight on a radius-8 circle + one zoomed out at radius
+20), FP32 with binary16 SH.  A step is one full frame -- cull + depth key + compaction + projection
++ SH, depth sort, tile binning, tile sort, tile raster + blend -- for camera (step mod 9).  Inputs
+(816 MB of splat buffers) are resident in HBM and larger than L2, so no L2 flush is interposed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank renders its own frames (replicas: one frame does not shard) and
+the line reports the whole-job frames/s.  --impl reference times the reference algorithm's CPU
+restatement (the oracle) on the host cores instead; the reference's own Vulkan shaders cannot run
+on this machine (no graphics stack).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at 6M splats 1600x900"
+UNIT = "frames/s"
+OPS_PER_FRAGMENT = 20  # FP32 lane-ops per covered (pixel, splat) pair, the blend's algorithmic cost
+WORKLOAD = "large"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=27)
+    p.add_argument("--warmup", type=int, default=9)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--splats", type=int, default=None, help="override the splat count (testing only)")
+    p.add_argument("--cpu-band-stride", type=int, default=8, help="CPU sample: blend every k-th 16-row band")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        if not self.rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in self.rows if num(r[1])]
+        mx = [num(r[2]) for r in self.rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic():
+    """dram bytes per raster launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "raster_large.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def make_scene(n_override=None):
+    from vkgs_gb300 import synthetic as syn
+
+    spec = syn.WORKLOADS[WORKLOAD]
+    n = spec["n"] if n_override is None else n_override
+    rows = syn.splat_rows(n, spec["seed"], spec["layout"])
+    return rows, syn.ply_offsets(), syn.workload_cameras(WORKLOAD), n
+
+
+def cpu_frames(oracle, act, cams, band_stride: int, steps: int, threads: int):
+    """Estimated seconds per frame on the host: full rank/sort/project + a band-sampled blend x stride."""
+    from tests import scenes
+
+    out = []
+    for k in range(steps):
+        spec = cams[k % len(cams)]
+        c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=spec.width, height=spec.height,
+                          near=spec.near, far=spec.far)
+        cam = scenes.oracle_camera(oracle, c)
+        t0 = time.perf_counter()
+        key, idx = oracle.rank(act[0], cam)
+        key, idx = oracle.sort_kv(key, idx)
+        _, rec = oracle.project(*act, idx, cam)
+        t1 = time.perf_counter()
+        oracle.raster_bands(rec, spec.width, spec.height, band_stride, k % band_stride)
+        t2 = time.perf_counter()
+        out.append((t1 - t0) + band_stride * (t2 - t1))
+    return out
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle
+
+    oracle.build()
+    rows, off, cams, n = make_scene(args.splats)
+    act = oracle.parse_ply(rows, off)
+    del rows
+    threads = oracle.num_threads()
+    cpu_frames(oracle, act, cams, args.cpu_band_stride, max(args.warmup, 0), threads)
+    times = cpu_frames(oracle, act, cams, args.cpu_band_stride, args.steps, threads)
+    value = len(times) / sum(times)
+    sample = (f"per step: full cull/key/sort/projection of all {n} splats + blend of every "
+              f"{args.cpu_band_stride}th 16-row band, blend time x{args.cpu_band_stride}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD}: {n} splats, 1600x900, 9 cameras (8 on r=8 circle + r=20)",
+                   "l2": "inputs (816 MB) exceed L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's Vulkan shaders cannot run here (no graphics stack); this arm is the scalar "
+                "C restatement of those shaders (oracle/cpu_ref.c) on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from vkgs_gb300 import build as vbuild
+
+    vbuild.build()
+    from vkgs_gb300 import Camera, Renderer, parse_ply
+    from vkgs_gb300 import _lib as L
+
+    rows, off, specs, n = make_scene(args.splats)
+    rows_t = torch.from_numpy(rows).to(dev)
+    host_rows = rows if (rank == 0 and not args.no_cpu_baseline) else None
+    del rows
+    splats = parse_ply(rows_t, off)
+    del rows_t
+    cams = [Camera.from_spec(s) for s in specs]
+    W, H = specs[0].width, specs[0].height
+    r = Renderer(n, W, H)
+    color = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+
+    # Untimed: size the tile-pair capacity and count each camera's fragments F.
+    r.count_fragments(True)
+    stats = []
+    for cam in cams:
+        _, st = r.render_checked(splats, cam, color=color)
+        stats.append(st)
+    r.count_fragments(False)
+    r.reserve(max_tile_pairs=int(max(s["tile_pairs"] for s in stats) * 1.05) + 1024)
+    for k in range(max(args.warmup, 3)):
+        r.render(splats, cams[k % len(cams)], color=color)
+    r.check()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    K = args.steps
+    r.enable_timing(True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(K):
+        r.render(splats, cams[k % len(cams)], color=color)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop() if clocks else None
+    r.check()
+    ms = e0.elapsed_time(e1)
+    stage = r.stage_times(K)
+    r.enable_timing(False)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * K / (ms_max / 1000.0)
+
+    # End to end through the public API: per step the camera crosses into the kernel parameters
+    # (h2d) and the finished RGBA image is copied into pinned host memory (d2h).
+    host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+    barrier()
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(K):
+        r.render(splats, cams[k % len(cams)], color=color)
+        host.copy_(color, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    te = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * K / (float(te.item()) / 1000.0)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    # Roofline of the dominant kernel (the raster/blend: FP32 issue-bound) + the HBM-bound stages.
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = sms * 128 * sm_max * 1e6 / 1e12  # T lane-ops/s
+    cam_of = [k % len(cams) for k in range(K)]
+    frags = np.array([stats[c]["fragments"] for c in cam_of], np.float64)
+    vis = np.array([stats[c]["visible_count"] for c in cam_of], np.float64)
+    raster_ms = stage[:, 5].astype(np.float64)
+    achieved = float((frags * OPS_PER_FRAGMENT).sum() / (raster_ms.sum() / 1e3) / 1e12)
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    cull_bytes = 12.0 * n + (8.0 + 188.0) * vis
+    sort_bytes = 64.0 * vis
+    stage_mean = {name: float(stage[:, i].mean()) for i, name in enumerate(L.STAGES)}
+    hbm_stages = {
+        "cull_project": {"ms": stage_mean["cull_project"],
+                         "gbs": float(cull_bytes.sum() / (stage[:, 0].sum() / 1e3) / 1e9)},
+        "depth_sort": {"ms": stage_mean["depth_sort"], "gbs": float(sort_bytes.sum() / (stage[:, 1].sum() / 1e3) / 1e9)},
+    }
+    for v in hbm_stages.values():
+        v["frac"] = v["gbs"] / hbm
+    dominant = max(stage_mean, key=stage_mean.get)
+
+    cpu = None
+    if host_rows is not None:
+        try:
+            from oracle import oracle
+
+            oracle.build()
+            act = oracle.parse_ply(host_rows, off)
+            del host_rows
+            threads = oracle.num_threads()
+            times = cpu_frames(oracle, act, specs, args.cpu_band_stride, len(specs), threads)
+            cpu = {"value": len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"each of the 9 cameras once: full cull/key/sort/projection + blend of every "
+                             f"{args.cpu_band_stride}th 16-row band, blend time x{args.cpu_band_stride}"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {exc}"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD}: {n} splats (70% shell r=4, 30% uniform), 1600x900, 9 cameras "
+                               "(8 on an r=8 circle + 1 at r=20), SH degree 3 in binary16",
+                   "parallelism": f"replicas x{world}", "l2": "inputs (816 MB) exceed L2; no flush"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 292, "d2h_bytes_per_step": H * W * 16},
+        "gpu_launches": None,
+        "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "T lane-ops/s", "frac": achieved / fp32_peak, "traffic": profile_traffic(),
+                     "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
+                     "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair"},
+        "roofline_hbm": {**hbm_stages, "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "stages_ms": stage_mean,
+        "dominant_stage": dominant,
+        "frame_stats": {"visible": [s["visible_count"] for s in stats], "tile_pairs": [s["tile_pairs"] for s in stats],
+                        "fragments": [s["fragments"] for s in stats]},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    # cull_project, depth sort (histogram + 4 passes), bin, tile sort (histogram + 2 passes), ranges, raster
+    launches_per_frame = 1 + 5 + 1 + 3 + 1 + 1
+    line["gpu_launches"] = launches_per_frame * K
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

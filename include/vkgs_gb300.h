@@ -1,0 +1,218 @@
+/*
+ * vkgs_gb300.h -- C ABI of the GB300 (sm_103a) splat pipeline.
+ *
+ * A drop-in for the per-frame compute-and-indirect-draw path of the vkgs
+ * viewer: rank (cull + depth key) -> radix sort -> projection (+SH) -> quad
+ * raster + SRC_ALPHA/ONE_MINUS_SRC_ALPHA blend, reimplemented as CUDA kernels.
+ * Plain pointers and sizes only; every device pointer is a CUDA device address.
+ * All calls that take a stream are asynchronous and stream-ordered; they never
+ * synchronise the host.  Device-side failures (a bounded wait that gave up, a
+ * capacity overflow) are recorded on the device and returned by
+ * gs_context_check().
+ *
+ * Reference interfaces replaced (paths within jaesung-cs/vkgs):
+ *   gs_sorter_*                    vrdxCreateSorter / vrdxGetSorterKeyValueStorageRequirements /
+ *                                  vrdxCmdSortKeyValueIndirect / vrdxDestroySorter
+ *                                  (src/vkgs/engine/engine.cc:509-521, 1218-1219, 531)
+ *   gs_render                      the frame sequence of Engine::Impl::Draw: rank dispatch, sort,
+ *                                  inverse map, projection dispatch, indexed-indirect splat draw
+ *                                  (src/vkgs/engine/engine.cc:1164-1290, 1380-1498)
+ *   gs_parse_ply                   the parse_ply.comp dispatch (engine.cc:1125-1162,
+ *                                  src/shader/parse_ply.comp:34-97)
+ *   gs_ply_offsets_from_header     the header walk + offset table of SplatLoadThread
+ *                                  (src/vkgs/engine/splat_load_thread.cc:53-135)
+ *   gs_camera_*                    vkgs::Camera::ProjectionMatrix / ViewMatrix / Eye
+ *                                  (src/vkgs/scene/camera.cc:25-45)
+ */
+#ifndef VKGS_GB300_H
+#define VKGS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* gs_stream;
+
+typedef enum gs_status {
+  GS_SUCCESS = 0,
+  GS_ERROR_INVALID_ARGUMENT = 1, /* null pointer, zero size where one is required, bad layout */
+  GS_ERROR_CAPACITY = 2,         /* a size beyond what the context/storage was reserved for */
+  GS_ERROR_CUDA = 3,             /* a CUDA runtime call or kernel launch failed */
+  GS_ERROR_DEVICE_TIMEOUT = 4,   /* a bounded device-side wait gave up (results of that call are invalid) */
+  GS_ERROR_OUT_OF_MEMORY = 5,    /* device allocation failed while reserving */
+} gs_status;
+
+/* Short text for a status code (static storage). */
+const char* gs_status_string(gs_status status);
+
+/* ------------------------------------------------------------------------ */
+/* Sorter: ascending 32-bit key sort carrying 32-bit values, count on device */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gs_sorter gs_sorter;
+
+/* vrdxCreateSorter (engine.cc:509-514).  Binds to the current CUDA device. */
+gs_status gs_sorter_create(gs_sorter** sorter);
+
+/* vrdxDestroySorter (engine.cc:531). */
+void gs_sorter_destroy(gs_sorter* sorter);
+
+/* vrdxGetSorterKeyValueStorageRequirements (engine.cc:517-519): scratch bytes for sorting up to
+ * max_count pairs. */
+gs_status gs_sorter_key_value_storage_requirements(gs_sorter* sorter, uint32_t max_count, size_t* bytes);
+
+/* vrdxCmdSortKeyValueIndirect (engine.cc:1218-1219): sorts keys[0..*count) ascending in place and
+ * permutes values alongside; equal keys keep their input order (stable).  count lives in device
+ * memory and is read on the device (no host sync); *count > max_count is clamped to max_count and
+ * recorded as GS_ERROR_CAPACITY on the device.  storage must hold the bytes reported for max_count
+ * and must not be used by another sort in flight. */
+gs_status gs_sorter_sort_key_value_indirect(gs_sorter* sorter, gs_stream stream, uint32_t max_count,
+                                            const uint32_t* count, uint32_t* keys, uint32_t* values,
+                                            void* storage, size_t storage_bytes);
+
+/* Reads back and clears the sorter's device error word (synchronises the stream). */
+gs_status gs_sorter_check(gs_sorter* sorter, gs_stream stream);
+
+/* ------------------------------------------------------------------------ */
+/* Splat buffers, camera, target                                             */
+/* ------------------------------------------------------------------------ */
+
+/* The reference's SoA splat storage (engine.cc:1639-1651), device pointers. */
+typedef struct gs_splats {
+  const float* position; /* N x 3 */
+  const float* cov3d;    /* N x 6: (00, 10, 20, 11, 21, 22) of the 3D covariance */
+  const float* opacity;  /* N, already sigmoid-activated */
+  const uint16_t* sh;    /* N x 48 IEEE binary16, [channel][16 coefficients] */
+  uint32_t count;
+} gs_splats;
+
+/* Writable form of the same buffers, filled by gs_parse_ply. */
+typedef struct gs_splat_buffers {
+  float* position;
+  float* cov3d;
+  float* opacity;
+  uint16_t* sh;
+} gs_splat_buffers;
+
+/* The Camera uniform (src/vkgs/vulkan/shader/uniforms.h:10-15) plus the model push constant
+ * (src/shader/rank.comp:13).  Matrices are column-major, like glm::mat4. */
+typedef struct gs_camera {
+  float projection[16];
+  float view[16];
+  float camera_position[3];
+  uint32_t width;  /* screen_size.x */
+  uint32_t height; /* screen_size.y */
+  float model[16];
+} gs_camera;
+
+/* Colour (+ optional depth) attachment.  At least one colour pointer must be set.
+ * The colour attachment is cleared to (0,0,0,1) and splats blend over it in sorted order. */
+typedef struct gs_target {
+  float* color_rgba32f;    /* H x W x 4 floats, row 0 = top (Vulkan framebuffer origin), or NULL */
+  uint8_t* color_bgra8;    /* H x W x 4 bytes B,G,R,A (B8G8R8A8_UNORM of the swapchain), or NULL */
+  const float* depth;      /* H x W D32 depth tested with LESS and not written, or NULL = cleared 1.0 */
+} gs_target;
+
+/* Optional per-frame outputs, all device pointers (NULL = not requested). */
+typedef struct gs_frame_outputs {
+  uint32_t* visible_count; /* 1 word: V */
+  uint32_t* keys;          /* N words; [0, V) = sorted depth keys floatBitsToUint(1 - ndc.z) */
+  uint32_t* index;         /* N words; [0, V) = splat ids in sorted order */
+  float* instances;        /* N x 12 floats; [0, V) = projection.comp instance records in sorted order */
+  uint32_t* draw_indirect; /* 12 words: the indirect draw arguments of projection.comp:64-75 */
+} gs_frame_outputs;
+
+/* ------------------------------------------------------------------------ */
+/* Render context                                                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gs_context gs_context;
+
+typedef struct gs_context_options {
+  uint32_t max_splats;      /* N capacity (the reference preallocates MAX_SPLAT_COUNT = 2^23) */
+  uint32_t max_width;       /* largest target width */
+  uint32_t max_height;      /* largest target height */
+  uint32_t max_tile_pairs;  /* (splat, tile) pair capacity; 0 = 16 * max_splats */
+} gs_context_options;
+
+typedef struct gs_frame_stats {
+  uint32_t visible_count;   /* V of the last frame */
+  uint32_t tile_pairs;      /* (splat, tile) pairs the last frame needed */
+  uint64_t fragments;       /* covered (pixel, splat) pairs, only with gs_context_set_count_fragments(1) */
+} gs_frame_stats;
+
+/* Creates a context on the current CUDA device and reserves all scratch for the given capacities. */
+gs_status gs_context_create(gs_context** context, const gs_context_options* options);
+void gs_context_destroy(gs_context* context);
+
+/* Grows the reserved scratch (never shrinks).  Synchronises the device; not for use inside capture. */
+gs_status gs_context_reserve(gs_context* context, const gs_context_options* options);
+
+/* Makes every following gs_render also count fragments (slower; for statistics and tests). */
+gs_status gs_context_set_count_fragments(gs_context* context, int enable);
+
+/* One frame.  No allocation, no host synchronisation: safe to capture in a CUDA graph once the
+ * context holds enough capacity. */
+gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camera* camera,
+                    const gs_target* target, const gs_frame_outputs* outputs, gs_stream stream);
+
+/* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
+ * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
+ * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,
+ * tile binning, tile sort, tile ranges, raster + blend. */
+#define GS_NUM_STAGES 6
+gs_status gs_context_enable_timing(gs_context* context, int enable);
+
+/* Synchronises the device, then writes up to max_frames rows of GS_NUM_STAGES milliseconds (oldest
+ * first) for the frames rendered since timing was enabled, and clears the record.  *frames receives
+ * the number of rows written. */
+gs_status gs_context_stage_times(gs_context* context, uint32_t max_frames, float* ms, uint32_t* frames);
+
+/* Synchronises the stream, then returns (and clears) the device error word of the last frames:
+ * GS_ERROR_CAPACITY when the tile pairs overflowed (stats->tile_pairs says how many are needed),
+ * GS_ERROR_DEVICE_TIMEOUT when a bounded wait gave up.  stats may be NULL. */
+gs_status gs_context_check(gs_context* context, gs_stream stream, gs_frame_stats* stats);
+
+/* ------------------------------------------------------------------------ */
+/* Loader: PLY header and parameter activation                               */
+/* ------------------------------------------------------------------------ */
+
+/* Walks an ASCII PLY header (up to and including "end_header") and fills the 60-word offset table of
+ * splat_load_thread.cc:114-135 (float offsets of x..z, scale_0..2, rot_1,rot_2,rot_3,rot_0, the 48 SH
+ * terms in [channel][coefficient] order, opacity, and the row stride at [59]).  Every property must
+ * be "float".  *header_bytes receives the size of the header including its final newline. */
+gs_status gs_ply_offsets_from_header(const char* text, size_t length, uint32_t offsets[60],
+                                     uint64_t* point_count, size_t* header_bytes);
+
+/* parse_ply.comp: activates count PLY rows (device, offsets[59] floats each) into the splat buffers:
+ * s = exp(log s), q normalised, cov3d = R S^2 R^T, SH to binary16 (round to nearest even),
+ * opacity = sigmoid. */
+gs_status gs_parse_ply(const float* rows, uint32_t count, const uint32_t offsets[60],
+                       const gs_splat_buffers* out, gs_stream stream);
+
+/* ------------------------------------------------------------------------ */
+/* Camera helpers (host only)                                                */
+/* ------------------------------------------------------------------------ */
+
+/* glm::perspective(fovy, aspect, near, far) (right-handed, clip z in [-1,1]) followed by the
+ * gl-to-vulkan conversion of camera.cc:29-34 (y flipped, z' = z/2 + w/2). */
+void gs_camera_perspective(float fovy, float aspect, float znear, float zfar, float out[16]);
+
+/* glm::lookAt(eye, center, up), right-handed. */
+void gs_camera_look_at(const float eye[3], const float center[3], const float up[3], float out[16]);
+
+/* Camera::Eye: center + r * (sin phi sin theta, cos phi, sin phi cos theta). */
+void gs_camera_orbit_eye(const float center[3], float r, float phi, float theta, float out[3]);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+uint32_t gs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VKGS_GB300_H */

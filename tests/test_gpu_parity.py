@@ -1,0 +1,289 @@
+"""GPU parity: the CUDA path (called through the C ABI) against the CPU oracle on identical inputs.
+
+Bars: visible count, sorted keys and sorted index bit-exact (tie rule: ascending splat id);
+projection instance records bit-exact (float equality, NaN == NaN); fragment count exact; images
+within 1/255 per channel of the oracle's FP32 image (IMAGE_TOL).
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from tests import scenes
+from vkgs_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+IMAGE_TOL = 1.0 / 255.0
+
+
+def render_gpu(act, c, depth=None, count_fragments=True, renderer=None, bgra=False):
+    import torch
+    from vkgs_gb300 import Renderer, Splats
+
+    pos, cov, opa, sh = act
+    sp = Splats.from_numpy(pos, cov, opa, sh)
+    n = sp.count
+    r = renderer or Renderer(max(n, 1), c["width"], c["height"])
+    r.count_fragments(count_fragments)
+    dev = sp.position.device
+    keys = torch.full((max(n, 1),), -1, dtype=torch.int32, device=dev)
+    index = torch.full((max(n, 1),), -1, dtype=torch.int32, device=dev)
+    inst = torch.zeros(max(n, 1) * 12, dtype=torch.float32, device=dev)
+    vc = torch.zeros(1, dtype=torch.int32, device=dev)
+    draw = torch.zeros(12, dtype=torch.int32, device=dev)
+    d = None if depth is None else torch.from_numpy(depth).to(dev)
+    b8 = torch.zeros((c["height"], c["width"], 4), dtype=torch.uint8, device=dev) if bgra else None
+    img = r.render(sp, scenes.product_camera(c), keys=keys, index=index, instances=inst, visible_count=vc,
+                   draw_indirect=draw, depth=d, bgra8=b8, color=torch.empty((c["height"], c["width"], 4),
+                                                                                 dtype=torch.float32, device=dev))
+    stats = r.check()
+    v = int(vc.item())
+    return dict(count=v, key=keys[:v].cpu().numpy().view(np.uint32), index=index[:v].cpu().numpy().view(np.uint32),
+                instance=inst[: v * 12].cpu().numpy().reshape(v, 12), image=img.cpu().numpy(),
+                fragments=stats["fragments"], stats=stats, draw=draw.cpu().numpy(),
+                bgra=None if b8 is None else b8.cpu().numpy())
+
+
+def render_cpu(oracle, act, c, depth=None):
+    pos, cov, opa, sh = act
+    return oracle.render_frame(pos, cov, opa, sh, scenes.oracle_camera(oracle, c), depth_in=depth)
+
+
+def assert_parity(g, o, image_tol=IMAGE_TOL):
+    assert g["count"] == o["count"]
+    np.testing.assert_array_equal(g["key"], o["key"])
+    np.testing.assert_array_equal(g["index"], o["index"])
+    np.testing.assert_array_equal(g["instance"][:, [0, 1, 2, 4, 5, 6, 7, 8, 9, 10, 11]],
+                                  o["instance"][:, [0, 1, 2, 4, 5, 6, 7, 8, 9, 10, 11]])
+    assert g["fragments"] == o["fragments"]
+    err = np.abs(g["image"].astype(np.float64) - o["image"])
+    assert err.max() <= image_tol, f"max image error {err.max()}"
+    v = g["count"]
+    np.testing.assert_array_equal(g["draw"], [6 * v, 1, 0, 0, 0, 0, 0, 0, v, 1, 0, 0])
+    return float(err.max())
+
+
+def test_small_workload_parity(cuda, oracle):
+    rows = syn.splat_rows(100_000, 0)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0))
+    g = render_gpu(act, c)
+    o = render_cpu(oracle, act, c)
+    err = assert_parity(g, o)
+    assert g["count"] > 90_000
+    assert err < 1e-4
+
+
+@pytest.mark.parametrize("n,w,h,seed", [(1, 64, 48, 0), (2, 33, 17, 1), (1023, 257, 131, 2), (1025, 160, 90, 3),
+                                        (4097, 320, 200, 4), (33_333, 500, 301, 5)])
+def test_ragged_sizes(cuda, oracle, n, w, h, seed):
+    rows = syn.splat_rows(n, seed)
+    act = scenes.activated(oracle, rows)
+    rng = np.random.default_rng(seed)
+    eye = rng.normal(size=3)
+    eye = eye / np.linalg.norm(eye) * rng.uniform(2.0, 8.0)
+    if abs(eye[1]) > 0.99 * np.linalg.norm(eye):
+        eye[0] += 1.0
+    c = scenes.camera(oracle, tuple(eye), fovy_deg=float(rng.uniform(40, 75)), width=w, height=h)
+    assert_parity(render_gpu(act, c), render_cpu(oracle, act, c))
+
+
+def test_empty_scene(cuda, oracle):
+    act = (np.zeros((0, 3), np.float32), np.zeros((0, 6), np.float32), np.zeros(0, np.float32),
+           np.zeros((0, 48), np.uint16))
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=100, height=60)
+    g = render_gpu(act, c)
+    assert g["count"] == 0
+    exp = np.zeros((60, 100, 4), np.float32)
+    exp[..., 3] = 1.0
+    np.testing.assert_array_equal(g["image"], exp)
+
+
+def test_everything_culled(cuda, oracle):
+    rows = syn.splat_rows(5000, 9)
+    rows[:, 2] += 50.0  # all splats behind a camera at z=6 looking at -z
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), center=(0.0, 0.0, 0.0), width=200, height=100)
+    g = render_gpu(act, c)
+    o = render_cpu(oracle, act, c)
+    assert g["count"] == o["count"] == 0
+    np.testing.assert_array_equal(g["image"], o["image"])
+
+
+def test_equal_depth_keys_keep_ascending_id(cuda, oracle):
+    # 20,000 splats on one plane facing the camera: massive key ties
+    rng = np.random.default_rng(3)
+    rows = syn.splat_rows(20_000, 3)
+    rows[:, 0:2] = rng.uniform(-2, 2, (20_000, 2))
+    rows[:, 2] = 0.0
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=320, height=180)
+    g = render_gpu(act, c)
+    o = render_cpu(oracle, act, c)
+    assert len(np.unique(g["key"])) < g["count"] // 10
+    assert_parity(g, o)
+
+
+def test_degenerate_and_far_plane_splats(cuda, oracle):
+    rows = scenes.rows_from([
+        scenes.single_splat((0, 0, 0), scale=(0.05, 0.05, 0.05)),    # D == 0 on a square target -> not drawn
+        scenes.single_splat((0.3, 0.1, 0), scale=(0.08, 0.02, 0.05)),
+        scenes.single_splat((0, 0, -93.9), scale=(0.5, 0.5, 0.5)),    # near the far plane
+        scenes.single_splat((0, 0, -94.1), scale=(0.5, 0.5, 0.5)),    # beyond it
+    ])
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=128, height=128)
+    assert_parity(render_gpu(act, c), render_cpu(oracle, act, c))
+
+
+def test_depth_input(cuda, oracle):
+    rows = syn.splat_rows(20_000, 6)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (1.0, 0.5, 5.0), width=300, height=200)
+    rng = np.random.default_rng(6)
+    depth = rng.uniform(0.975, 1.0, (200, 300)).astype(np.float32)
+    g = render_gpu(act, c, depth=depth)
+    o = render_cpu(oracle, act, c, depth=depth)
+    assert_parity(g, o)
+
+
+def test_bgra8_target_is_quantised_rgba(cuda, oracle):
+    rows = syn.splat_rows(10_000, 8)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=200, height=120)
+    g = render_gpu(act, c, bgra=True)
+    q = np.clip(np.rint(np.clip(g["image"], 0, 1) * 255), 0, 255).astype(np.int32)
+    b = g["bgra"].astype(np.int32)
+    np.testing.assert_array_equal(b[..., [2, 1, 0, 3]], q)
+
+
+def test_model_transform(cuda, oracle):
+    rows = syn.splat_rows(20_000, 12)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.5, 1.0, 6.0), width=320, height=240, model=scenes.rotation_model())
+    g = render_gpu(act, c)
+    o = render_cpu(oracle, act, c)
+    assert g["count"] == o["count"]
+    np.testing.assert_array_equal(g["key"], o["key"])
+    np.testing.assert_array_equal(g["index"], o["index"])
+    np.testing.assert_allclose(g["instance"], o["instance"], rtol=1e-6, atol=1e-7)
+    assert np.abs(g["image"] - o["image"]).max() <= IMAGE_TOL
+
+
+def test_render_is_deterministic(cuda, oracle):
+    rows = syn.splat_rows(50_000, 4)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 1.0, 5.0), width=400, height=300)
+    a = render_gpu(act, c)
+    b = render_gpu(act, c)
+    np.testing.assert_array_equal(a["image"], b["image"])
+    np.testing.assert_array_equal(a["index"], b["index"])
+
+
+def test_tile_pair_overflow_is_reported_and_recoverable(cuda, oracle):
+    import torch
+    from vkgs_gb300 import GsError, Renderer, Splats
+
+    rows = syn.splat_rows(20_000, 1)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=320, height=180)
+    r = Renderer(20_000, 320, 180, max_tile_pairs=1000)
+    sp = Splats.from_numpy(*act)
+    r.render(sp, scenes.product_camera(c))
+    with pytest.raises(GsError) as e:
+        r.check()
+    assert e.value.status == 2 and e.value.stats["tile_pairs"] > 1000
+    img, stats = r.render_checked(sp, scenes.product_camera(c))
+    o = render_cpu(oracle, act, c)
+    assert np.abs(img.cpu().numpy() - o["image"]).max() <= IMAGE_TOL
+
+
+def test_capacity_checks(cuda):
+    from vkgs_gb300 import GsError, Renderer, Splats
+
+    r = Renderer(10, 64, 64)
+    sp = Splats.empty(11)
+    from vkgs_gb300 import Camera
+
+    cam = Camera.look_at((0, 0, 6), width=64, height=64)
+    with pytest.raises(GsError) as e:
+        r.render(sp, cam)
+    assert e.value.status == 2
+    with pytest.raises(GsError):
+        r.render(Splats.empty(5), Camera.look_at((0, 0, 6), width=65, height=64))
+
+
+def test_parse_ply_on_gpu(cuda, oracle):
+    import torch
+    from vkgs_gb300 import parse_ply
+
+    rows = syn.splat_rows(50_000, 13)
+    off = syn.ply_offsets()
+    sp = parse_ply(torch.from_numpy(rows).cuda(), off)
+    pos, cov, opa, sh = oracle.parse_ply(rows, off)
+    np.testing.assert_array_equal(sp.position.cpu().numpy(), pos)
+    np.testing.assert_array_equal(sp.sh.cpu().numpy().view(np.uint16), sh)
+    np.testing.assert_allclose(sp.cov3d.cpu().numpy(), cov, rtol=2e-6, atol=1e-12)
+    np.testing.assert_allclose(sp.opacity.cpu().numpy(), opa, rtol=1e-6)
+
+
+def test_load_ply_file_roundtrip(cuda, oracle, tmp_path):
+    from vkgs_gb300 import load, write_ply
+
+    rows = syn.splat_rows(3000, 14)
+    p = tmp_path / "scene.ply"
+    write_ply(p, rows, syn.PLY_PROPERTIES)
+    sp = load(p)
+    pos, cov, opa, sh = oracle.parse_ply(rows, syn.ply_offsets())
+    np.testing.assert_array_equal(sp.position.cpu().numpy(), pos)
+    np.testing.assert_array_equal(sp.sh.cpu().numpy().view(np.uint16), sh)
+
+
+@pytest.mark.parametrize("n,count", [(1, 1), (4096, 4096), (4097, 3000), (300_000, 299_999), (1 << 20, 1 << 20)])
+def test_sorter_matches_stable_sort(cuda, n, count):
+    import torch
+    from vkgs_gb300 import Sorter
+
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 3] = keys[n // 3: 2 * (n // 3)]  # plenty of duplicates
+    vals = np.arange(n, dtype=np.uint32)
+    kt = torch.from_numpy(keys.view(np.int32)).cuda()
+    vt = torch.from_numpy(vals.view(np.int32)).cuda()
+    s = Sorter()
+    s.sort_key_value(kt, vt, count=count)
+    s.check()
+    order = np.argsort(keys[:count], kind="stable")
+    np.testing.assert_array_equal(kt.cpu().numpy().view(np.uint32)[:count], keys[:count][order])
+    np.testing.assert_array_equal(vt.cpu().numpy().view(np.uint32)[:count], vals[:count][order])
+    np.testing.assert_array_equal(kt.cpu().numpy().view(np.uint32)[count:], keys[count:])
+
+
+def test_sorter_count_beyond_capacity_is_reported(cuda):
+    import torch
+    from vkgs_gb300 import GsError, Sorter
+
+    kt = torch.arange(1000, 0, -1, dtype=torch.int32, device="cuda")
+    vt = torch.arange(1000, dtype=torch.int32, device="cuda")
+    s = Sorter()
+    s.sort_key_value(kt, vt, count=torch.tensor([5000], dtype=torch.int32, device="cuda"))
+    with pytest.raises(GsError) as e:
+        s.check()
+    assert e.value.status == 2
+    k = kt.cpu().numpy()
+    assert np.all(k[:-1] <= k[1:])  # clamped to max_count and still sorted
+
+
+@pytest.mark.parametrize("cam_index", [0, 8])
+def test_large_workload_parity(cuda, oracle, cam_index):
+    """6M splats (shell layout), one circle camera and the zoomed-out camera, at full size."""
+    rows = syn.splat_rows(6_000_000, 1, "shell")
+    act = scenes.activated(oracle, rows)
+    del rows
+    spec = syn.circle_cameras()[cam_index]
+    c = scenes.camera(oracle, spec.eye, width=spec.width, height=spec.height)
+    g = render_gpu(act, c)
+    o = render_cpu(oracle, act, c)
+    assert_parity(g, o)

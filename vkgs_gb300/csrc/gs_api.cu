@@ -1,0 +1,752 @@
+// gs_api.cu -- the C ABI: render context, frame orchestration, sorter, loader and camera helpers.
+//
+// The frame sequence replaces Engine::Impl::Draw's compute + draw recording
+// (src/vkgs/engine/engine.cc:1164-1290 and DrawNormalPass 1380-1498):
+//   reference                                  here
+//   fill(visible_count, 0) + rank.comp          cull + key + order-preserving compaction + projection
+//   vrdxCmdSortKeyValueIndirect                 onesweep radix sort of (key, index), count on device
+//   fill(inverse, -1) + inverse_index.comp      (not needed: records are keyed by splat id)
+//   projection.comp                             (fused into the cull pass)
+//   vkCmdDrawIndexedIndirect + blend            tile binning -> stable tile sort -> tile raster
+// Nothing here synchronises the host or allocates after gs_context_create/gs_context_reserve.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/vkgs_gb300.h"
+#include "gs_internal.h"
+
+using namespace gs;
+
+namespace {
+
+constexpr uint32_t kVersion = 1 * 10000 + 0 * 100 + 0;
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// A single device allocation carved into aligned sub-buffers.
+struct Carver {
+  size_t offset = 0;
+  char* base = nullptr;
+  template <typename T>
+  T* take(size_t count) {
+    T* p = reinterpret_cast<T*>(base ? base + offset : nullptr);
+    offset += align_up(count * sizeof(T) + 16);
+    return p;
+  }
+};
+
+u32 ceil_log2(u32 x) {
+  u32 b = 0;
+  while (b < 32 && (1ull << b) < x) ++b;
+  return b;
+}
+
+gs_status from_cuda(cudaError_t e) { return e == cudaSuccess ? GS_SUCCESS : GS_ERROR_CUDA; }
+
+// Frame-local device words (cleared at the start of every frame).
+enum FrameWord : u32 {
+  FW_VISIBLE = 0,
+  FW_PAIR_COUNT = 1,
+  FW_PAIR_TOTAL = 2,
+  FW_TICKET_CULL = 3,
+  FW_TICKET_BIN = 4,
+  FW_FRAGMENTS = 6,  // u64 at words 6..7
+  FW_WORDS = 16,
+};
+
+}  // namespace
+
+struct gs_context {
+  int device = 0;
+  int num_sms = 1;
+  u32 max_splats = 0, max_width = 0, max_height = 0, max_tiles = 0, pair_capacity = 0;
+  int count_fragments = 0;
+  u32 epoch = 1;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  // carved buffers
+  u32* frame = nullptr;  // FW_WORDS
+  u32* err = nullptr;
+  u32* key = nullptr;
+  u32* index = nullptr;
+  u32* key_alt = nullptr;
+  u32* index_alt = nullptr;
+  float4* record = nullptr;
+  float* inst_by_id = nullptr;
+  u64* cull_status = nullptr;
+  u64* bin_status = nullptr;
+  u32* radix_control = nullptr;
+  u64* radix_status = nullptr;
+  size_t radix_status_words = 0;
+  u32* pair_tile = nullptr;
+  u32* pair_splat = nullptr;
+  u32* pair_tile_alt = nullptr;
+  u32* pair_splat_alt = nullptr;
+  u32* tile_range = nullptr;
+  size_t status_bytes_begin = 0, status_bytes_end = 0;  // epoch-tagged region (zeroed on allocation)
+  // stage timing: a ring of kTimingRing frames x (GS_NUM_STAGES + 1) events
+  static constexpr u32 kTimingRing = 256;
+  bool timing = false;
+  cudaEvent_t* events = nullptr;
+  u32 timed_frames = 0;  // frames recorded since enabling (may exceed the ring)
+
+  cudaEvent_t* frame_events(u32 frame) { return events + (size_t)(frame % kTimingRing) * (GS_NUM_STAGES + 1); }
+
+  u32 take_epochs(u32 k) {
+    if (epoch > 0xffffff00u) {  // wrap: clear every epoch-tagged status word once
+      cudaMemset(arena + status_bytes_begin, 0, status_bytes_end - status_bytes_begin);
+      epoch = 1;
+    }
+    const u32 e = epoch;
+    epoch += k;
+    return e;
+  }
+};
+
+struct gs_sorter {
+  int device = 0;
+  int num_sms = 1;
+  u32* err = nullptr;  // device word
+};
+
+static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, u32 max_height, u32 max_pairs) {
+  const u32 tiles_x = (max_width + kTile - 1) / kTile, tiles_y = (max_height + kTile - 1) / kTile;
+  const u32 max_tiles = std::max(1u, tiles_x * tiles_y);
+  const u32 n = std::max(1u, max_splats);
+  const u32 pairs = std::max(1u, max_pairs);
+  Carver plan;
+  auto layout = [&](Carver& cv, gs_context* t) {
+    t->frame = cv.take<u32>(FW_WORDS);
+    t->err = cv.take<u32>(4);
+    t->key = cv.take<u32>(n);
+    t->index = cv.take<u32>(n);
+    t->key_alt = cv.take<u32>(n);
+    t->index_alt = cv.take<u32>(n);
+    t->record = cv.take<float4>((size_t)n * 4);
+    t->inst_by_id = cv.take<float>((size_t)n * 12);
+    t->tile_range = cv.take<u32>((size_t)max_tiles * 2);
+    t->radix_control = cv.take<u32>(kRadixControlBytes / sizeof(u32));
+    t->pair_tile = cv.take<u32>(pairs);
+    t->pair_splat = cv.take<u32>(pairs);
+    t->pair_tile_alt = cv.take<u32>(pairs);
+    t->pair_splat_alt = cv.take<u32>(pairs);
+    t->status_bytes_begin = cv.offset;
+    t->cull_status = cv.take<u64>((n + kCullTile - 1) / kCullTile);
+    t->bin_status = cv.take<u64>((n + kBinTile - 1) / kBinTile);
+    t->radix_status_words = radix_status_words(std::max(n, pairs));
+    t->radix_status = cv.take<u64>(t->radix_status_words);
+    t->status_bytes_end = cv.offset;
+  };
+  gs_context probe;
+  layout(plan, &probe);
+  char* arena = nullptr;
+  if (cudaMalloc(&arena, plan.offset) != cudaSuccess) {
+    cudaGetLastError();
+    return GS_ERROR_OUT_OF_MEMORY;
+  }
+  if (cudaMemset(arena, 0, plan.offset) != cudaSuccess) {
+    cudaFree(arena);
+    return GS_ERROR_CUDA;
+  }
+  if (c->arena) {
+    cudaDeviceSynchronize();
+    cudaFree(c->arena);
+  }
+  Carver real;
+  real.base = arena;
+  layout(real, c);
+  c->arena = arena;
+  c->arena_bytes = plan.offset;
+  c->max_splats = n;
+  c->max_width = max_width;
+  c->max_height = max_height;
+  c->max_tiles = max_tiles;
+  c->pair_capacity = pairs;
+  c->epoch = 1;
+  return GS_SUCCESS;
+}
+
+namespace gs {
+
+static void mat4_mul_host(const float a[16], const float b[16], float out[16]) {
+  float r[16];
+  for (int j = 0; j < 4; ++j)
+    for (int i = 0; i < 4; ++i)
+      r[j * 4 + i] = ((a[0 * 4 + i] * b[j * 4 + 0] + a[1 * 4 + i] * b[j * 4 + 1]) + a[2 * 4 + i] * b[j * 4 + 2]) +
+                     a[3 * 4 + i] * b[j * 4 + 3];
+  std::memcpy(out, r, sizeof(r));
+}
+
+// det and adjugate of a 4x4 (column-major) in double, by cofactor expansion.
+static void camera_in_model_space(const float model[16], const float eye[3], float out[3]) {
+  double m[4][4];  // m[row][col]
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r) m[r][c] = model[c * 4 + r];
+  auto minor3 = [&](int skip_r, int skip_c) {
+    double s[3][3];
+    for (int r = 0, rr = 0; r < 4; ++r) {
+      if (r == skip_r) continue;
+      for (int c = 0, cc = 0; c < 4; ++c) {
+        if (c == skip_c) continue;
+        s[rr][cc++] = m[r][c];
+      }
+      ++rr;
+    }
+    return s[0][0] * (s[1][1] * s[2][2] - s[1][2] * s[2][1]) - s[0][1] * (s[1][0] * s[2][2] - s[1][2] * s[2][0]) +
+           s[0][2] * (s[1][0] * s[2][1] - s[1][1] * s[2][0]);
+  };
+  double inv[4][4];  // inv[row][col] = cofactor(col,row) / det
+  double det = 0.0;
+  for (int c = 0; c < 4; ++c) det += ((c & 1) ? -1.0 : 1.0) * m[0][c] * minor3(0, c);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) inv[r][c] = (((r + c) & 1) ? -1.0 : 1.0) * minor3(c, r) / det;
+  const double e[4] = {eye[0], eye[1], eye[2], 1.0};
+  double p[4];
+  for (int r = 0; r < 4; ++r) p[r] = inv[r][0] * e[0] + inv[r][1] * e[1] + inv[r][2] * e[2] + inv[r][3] * e[3];
+  for (int i = 0; i < 3; ++i) out[i] = (float)(p[i] / p[3]);
+}
+
+void frame_constants(const float projection[16], const float view[16], const float model[16], const float eye[3],
+                     u32 width, u32 height, u32 n, FrameConst* fc) {
+  float pv[16];
+  mat4_mul_host(projection, view, pv);
+  mat4_mul_host(pv, model, fc->pvm);
+  std::memcpy(fc->model, model, 64);
+  std::memcpy(fc->view, view, 64);
+  std::memcpy(fc->proj, projection, 64);
+  bool ident = true;
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r) ident = ident && model[c * 4 + r] == (c == r ? 1.0f : 0.0f);
+  fc->model_identity = ident ? 1u : 0u;
+  if (ident) {
+    fc->cam_m[0] = eye[0], fc->cam_m[1] = eye[1], fc->cam_m[2] = eye[2];
+  } else {
+    camera_in_model_space(model, eye, fc->cam_m);
+  }
+  fc->lpx = 1.0f / (float)width / (float)width;
+  fc->lpy = 1.0f / (float)height / (float)height;
+  fc->width = width;
+  fc->height = height;
+  fc->n = n;
+}
+
+}  // namespace gs
+
+extern "C" {
+
+const char* gs_status_string(gs_status s) {
+  switch (s) {
+    case GS_SUCCESS: return "success";
+    case GS_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case GS_ERROR_CAPACITY: return "capacity exceeded";
+    case GS_ERROR_CUDA: return "CUDA error";
+    case GS_ERROR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case GS_ERROR_OUT_OF_MEMORY: return "out of device memory";
+  }
+  return "unknown status";
+}
+
+uint32_t gs_version(void) { return kVersion; }
+
+// ------------------------------------------------------------------ sorter
+
+gs_status gs_sorter_create(gs_sorter** out) {
+  if (!out) return GS_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  gs_sorter* s = new (std::nothrow) gs_sorter();
+  if (!s) return GS_ERROR_OUT_OF_MEMORY;
+  if (cudaGetDevice(&s->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
+    delete s;
+    return GS_ERROR_CUDA;
+  }
+  if (cudaMalloc(&s->err, 256) != cudaSuccess) {
+    delete s;
+    return GS_ERROR_OUT_OF_MEMORY;
+  }
+  cudaMemset(s->err, 0, 256);
+  *out = s;
+  return GS_SUCCESS;
+}
+
+void gs_sorter_destroy(gs_sorter* s) {
+  if (!s) return;
+  cudaFree(s->err);
+  delete s;
+}
+
+static size_t sorter_bytes(u32 max_count, size_t* status_off, size_t* alt_off) {
+  const size_t control = align_up(kRadixControlBytes);
+  const size_t status = align_up(radix_status_words(max_count) * sizeof(u64));
+  const size_t alt = align_up((size_t)std::max(max_count, 1u) * sizeof(u32));
+  if (status_off) *status_off = control;
+  if (alt_off) *alt_off = control + status;
+  return control + status + 2 * alt;
+}
+
+gs_status gs_sorter_key_value_storage_requirements(gs_sorter* s, uint32_t max_count, size_t* bytes) {
+  if (!s || !bytes) return GS_ERROR_INVALID_ARGUMENT;
+  *bytes = sorter_bytes(max_count, nullptr, nullptr);
+  return GS_SUCCESS;
+}
+
+gs_status gs_sorter_sort_key_value_indirect(gs_sorter* s, gs_stream stream, uint32_t max_count, const uint32_t* count,
+                                            uint32_t* keys, uint32_t* values, void* storage, size_t storage_bytes) {
+  if (!s || !count || !keys || !values || !storage) return GS_ERROR_INVALID_ARGUMENT;
+  size_t status_off = 0, alt_off = 0;
+  const size_t need = sorter_bytes(max_count, &status_off, &alt_off);
+  if (storage_bytes < need) return GS_ERROR_CAPACITY;
+  if (max_count == 0) return GS_SUCCESS;
+  char* base = static_cast<char*>(storage);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaMemsetAsync(base + status_off, 0, alt_off - status_off, st) != cudaSuccess) return GS_ERROR_CUDA;
+  const size_t alt_words = align_up((size_t)max_count * sizeof(u32)) / sizeof(u32);
+  RadixSortArgs a{};
+  a.keys = keys;
+  a.values = values;
+  a.keys_alt = reinterpret_cast<u32*>(base + alt_off);
+  a.values_alt = a.keys_alt + alt_words;
+  a.count = count;
+  a.max_count = max_count;
+  a.begin_bit = 0;
+  a.end_bit = 32;
+  a.control = reinterpret_cast<u32*>(base);
+  a.status = reinterpret_cast<u64*>(base + status_off);
+  a.epoch = 1;
+  a.err = s->err;
+  a.num_sms = s->num_sms;
+  return from_cuda(radix_sort(a, st));  // 4 passes: the result is back in keys/values
+}
+
+gs_status gs_sorter_check(gs_sorter* s, gs_stream stream) {
+  if (!s) return GS_ERROR_INVALID_ARGUMENT;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return GS_ERROR_CUDA;
+  u32 e = 0;
+  if (cudaMemcpy(&e, s->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return GS_ERROR_CUDA;
+  cudaMemset(s->err, 0, 4);
+  if (e & ERR_TIMEOUT) return GS_ERROR_DEVICE_TIMEOUT;
+  if (e & ERR_CAPACITY) return GS_ERROR_CAPACITY;
+  return GS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ context
+
+gs_status gs_context_create(gs_context** out, const gs_context_options* o) {
+  if (!out || !o) return GS_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (o->max_width == 0 || o->max_height == 0) return GS_ERROR_INVALID_ARGUMENT;
+  gs_context* c = new (std::nothrow) gs_context();
+  if (!c) return GS_ERROR_OUT_OF_MEMORY;
+  if (cudaGetDevice(&c->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
+    delete c;
+    return GS_ERROR_CUDA;
+  }
+  const u32 pairs = o->max_tile_pairs ? o->max_tile_pairs : (u32)std::min<uint64_t>(16ull * o->max_splats, 0x3fffffffull);
+  const gs_status st = context_allocate(c, o->max_splats, o->max_width, o->max_height, pairs);
+  if (st != GS_SUCCESS) {
+    delete c;
+    return st;
+  }
+  *out = c;
+  return GS_SUCCESS;
+}
+
+void gs_context_destroy(gs_context* c) {
+  if (!c) return;
+  if (c->arena) {
+    cudaDeviceSynchronize();
+    cudaFree(c->arena);
+  }
+  if (c->events) {
+    for (u32 i = 0; i < gs_context::kTimingRing * (GS_NUM_STAGES + 1); ++i) cudaEventDestroy(c->events[i]);
+    delete[] c->events;
+  }
+  delete c;
+}
+
+gs_status gs_context_enable_timing(gs_context* c, int enable) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  if (enable && !c->events) {
+    const u32 total = gs_context::kTimingRing * (GS_NUM_STAGES + 1);
+    c->events = new (std::nothrow) cudaEvent_t[total];
+    if (!c->events) return GS_ERROR_OUT_OF_MEMORY;
+    for (u32 i = 0; i < total; ++i) {
+      if (cudaEventCreate(&c->events[i]) != cudaSuccess) {
+        for (u32 j = 0; j < i; ++j) cudaEventDestroy(c->events[j]);
+        delete[] c->events;
+        c->events = nullptr;
+        return GS_ERROR_CUDA;
+      }
+    }
+  }
+  c->timing = enable != 0;
+  c->timed_frames = 0;
+  return GS_SUCCESS;
+}
+
+gs_status gs_context_stage_times(gs_context* c, uint32_t max_frames, float* ms, uint32_t* frames) {
+  if (!c || !frames || (max_frames && !ms)) return GS_ERROR_INVALID_ARGUMENT;
+  *frames = 0;
+  if (!c->events || c->timed_frames == 0) return GS_SUCCESS;
+  if (cudaDeviceSynchronize() != cudaSuccess) return GS_ERROR_CUDA;
+  const u32 kept = std::min(c->timed_frames, gs_context::kTimingRing);
+  const u32 rows = std::min(kept, max_frames);
+  const u32 first = c->timed_frames - kept;
+  for (u32 r = 0; r < rows; ++r) {
+    cudaEvent_t* ev = c->frame_events(first + r);
+    for (int s = 0; s < GS_NUM_STAGES; ++s) {
+      float t = 0.0f;
+      if (cudaEventElapsedTime(&t, ev[s], ev[s + 1]) != cudaSuccess) return GS_ERROR_CUDA;
+      ms[(size_t)r * GS_NUM_STAGES + s] = t;
+    }
+  }
+  *frames = rows;
+  c->timed_frames = 0;
+  return GS_SUCCESS;
+}
+
+gs_status gs_context_reserve(gs_context* c, const gs_context_options* o) {
+  if (!c || !o) return GS_ERROR_INVALID_ARGUMENT;
+  const u32 n = std::max(c->max_splats, o->max_splats);
+  const u32 w = std::max(c->max_width, o->max_width), h = std::max(c->max_height, o->max_height);
+  u32 pairs = std::max(c->pair_capacity, o->max_tile_pairs);
+  if (pairs > 0x3fffffffu) return GS_ERROR_CAPACITY;
+  if (n == c->max_splats && w == c->max_width && h == c->max_height && pairs == c->pair_capacity) return GS_SUCCESS;
+  if (cudaDeviceSynchronize() != cudaSuccess) return GS_ERROR_CUDA;
+  return context_allocate(c, n, w, h, pairs);
+}
+
+gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  c->count_fragments = enable ? 1 : 0;
+  return GS_SUCCESS;
+}
+
+gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, const gs_target* t,
+                    const gs_frame_outputs* outs, gs_stream stream) {
+  if (!c || !s || !cam || !t) return GS_ERROR_INVALID_ARGUMENT;
+  if (!t->color_rgba32f && !t->color_bgra8) return GS_ERROR_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (s->count && (!s->position || !s->cov3d || !s->opacity || !s->sh)) return GS_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(s->sh) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (s->count > c->max_splats || cam->width > c->max_width || cam->height > c->max_height) return GS_ERROR_CAPACITY;
+  if (s->count > 0x3fffffffu) return GS_ERROR_CAPACITY;
+  gs_frame_outputs none{};
+  const gs_frame_outputs& o = outs ? *outs : none;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const u32 n = s->count;
+  const u32 W = cam->width, H = cam->height;
+  const u32 tiles_x = (W + kTile - 1) / kTile, tiles_y = (H + kTile - 1) / kTile;
+  const u32 tiles = tiles_x * tiles_y;
+
+  FrameConst fc;
+  frame_constants(cam->projection, cam->view, cam->model, cam->camera_position, W, H, n, &fc);
+
+#define GS_TRY(x)                                  \
+  do {                                             \
+    if ((x) != cudaSuccess) return GS_ERROR_CUDA; \
+  } while (0)
+
+  cudaEvent_t* ev = c->timing ? c->frame_events(c->timed_frames++) : nullptr;
+#define GS_MARK(i) \
+  if (ev) GS_TRY(cudaEventRecord(ev[i], st))
+  GS_MARK(0);
+  GS_TRY(cudaMemsetAsync(c->frame, 0, FW_WORDS * sizeof(u32), st));
+  GS_TRY(cudaMemsetAsync(c->tile_range, 0, (size_t)tiles * 2 * sizeof(u32), st));
+  u32* key = o.keys ? o.keys : c->key;
+  u32* index = o.index ? o.index : c->index;
+  const bool want_inst = o.instances != nullptr;
+
+  CullArgs ca{};
+  ca.position = s->position;
+  ca.cov3d = s->cov3d;
+  ca.opacity = s->opacity;
+  ca.sh = s->sh;
+  ca.key = key;
+  ca.index = index;
+  ca.record = c->record;
+  ca.inst_by_id = want_inst ? c->inst_by_id : nullptr;
+  ca.visible_count = c->frame + FW_VISIBLE;
+  ca.status = c->cull_status;
+  ca.ticket = c->frame + FW_TICKET_CULL;
+  ca.epoch = c->take_epochs(1);
+  ca.err = c->err;
+  ca.num_sms = c->num_sms;
+  GS_TRY(launch_cull_project(fc, ca, st));
+  GS_MARK(1);
+
+  if (n > 0) {
+    RadixSortArgs ra{};
+    ra.keys = key;
+    ra.values = index;
+    ra.keys_alt = c->key_alt;
+    ra.values_alt = c->index_alt;
+    ra.count = c->frame + FW_VISIBLE;
+    ra.max_count = n;
+    ra.begin_bit = 0;
+    ra.end_bit = 32;
+    ra.control = c->radix_control;
+    ra.status = c->radix_status;
+    ra.epoch = c->take_epochs(4);
+    ra.err = c->err;
+    ra.num_sms = c->num_sms;
+    GS_TRY(radix_sort(ra, st));  // 4 passes: sorted keys/index are back in key/index
+  }
+
+  if (want_inst || o.draw_indirect)
+    GS_TRY(launch_instances(index, c->frame + FW_VISIBLE, c->inst_by_id, n, o.instances, o.draw_indirect, st));
+  GS_MARK(2);
+
+  BinArgs ba{};
+  ba.index = index;
+  ba.visible_count = c->frame + FW_VISIBLE;
+  ba.record = c->record;
+  ba.n = n;
+  ba.width = W;
+  ba.height = H;
+  ba.tiles_x = tiles_x;
+  ba.tiles_y = tiles_y;
+  ba.pair_tile = c->pair_tile;
+  ba.pair_splat = c->pair_splat;
+  ba.pair_capacity = c->pair_capacity;
+  ba.pair_count = c->frame + FW_PAIR_COUNT;
+  ba.pair_total = c->frame + FW_PAIR_TOTAL;
+  ba.status = c->bin_status;
+  ba.ticket = c->frame + FW_TICKET_BIN;
+  ba.epoch = c->take_epochs(1);
+  ba.err = c->err;
+  ba.num_sms = c->num_sms;
+  GS_TRY(launch_bin(ba, st));
+  GS_MARK(3);
+
+  const u32* sorted_tile = c->pair_tile;
+  const u32* sorted_splat = c->pair_splat;
+  const u32 tile_bits = ceil_log2(tiles);
+  if (n > 0 && tile_bits > 0) {
+    RadixSortArgs ra{};
+    ra.keys = c->pair_tile;
+    ra.values = c->pair_splat;
+    ra.keys_alt = c->pair_tile_alt;
+    ra.values_alt = c->pair_splat_alt;
+    ra.count = c->frame + FW_PAIR_COUNT;
+    ra.max_count = c->pair_capacity;
+    ra.begin_bit = 0;
+    ra.end_bit = tile_bits;
+    ra.control = c->radix_control;
+    ra.status = c->radix_status;
+    const u32 passes = radix_passes(0, tile_bits);
+    ra.epoch = c->take_epochs(passes);
+    ra.err = c->err;
+    ra.num_sms = c->num_sms;
+    GS_TRY(radix_sort(ra, st));
+    if (passes & 1u) {
+      sorted_tile = c->pair_tile_alt;
+      sorted_splat = c->pair_splat_alt;
+    }
+  }
+  GS_MARK(4);
+  if (n > 0) GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range,
+                                       c->num_sms, st));
+
+  RasterArgs rr{};
+  rr.tile_range = c->tile_range;
+  rr.pair_splat = sorted_splat;
+  rr.record = c->record;
+  rr.width = W;
+  rr.height = H;
+  rr.tiles_x = tiles_x;
+  rr.tiles_y = tiles_y;
+  rr.out_rgba = t->color_rgba32f;
+  rr.out_bgra = reinterpret_cast<uchar4*>(t->color_bgra8);
+  rr.depth = t->depth;
+  rr.t_floor = 5.9604645e-08f;  // 2^-24
+  rr.fragments = c->count_fragments ? reinterpret_cast<unsigned long long*>(c->frame + FW_FRAGMENTS) : nullptr;
+  GS_MARK(5);
+  GS_TRY(launch_raster(rr, st));
+  GS_MARK(6);
+
+  if (o.visible_count)
+    GS_TRY(cudaMemcpyAsync(o.visible_count, c->frame + FW_VISIBLE, sizeof(u32), cudaMemcpyDeviceToDevice, st));
+#undef GS_MARK
+#undef GS_TRY
+  return GS_SUCCESS;
+}
+
+gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stats) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return GS_ERROR_CUDA;
+  u32 words[FW_WORDS];
+  u32 e = 0;
+  if (cudaMemcpy(words, c->frame, sizeof(words), cudaMemcpyDeviceToHost) != cudaSuccess) return GS_ERROR_CUDA;
+  if (cudaMemcpy(&e, c->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return GS_ERROR_CUDA;
+  if (cudaMemset(c->err, 0, 4) != cudaSuccess) return GS_ERROR_CUDA;
+  if (stats) {
+    stats->visible_count = words[FW_VISIBLE];
+    stats->tile_pairs = words[FW_PAIR_TOTAL];
+    uint64_t f;
+    std::memcpy(&f, words + FW_FRAGMENTS, 8);
+    stats->fragments = f;
+  }
+  if (e & ERR_TIMEOUT) return GS_ERROR_DEVICE_TIMEOUT;
+  if (e & ERR_CAPACITY) return GS_ERROR_CAPACITY;
+  return GS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ loader
+
+gs_status gs_parse_ply(const float* rows, uint32_t count, const uint32_t offsets[60], const gs_splat_buffers* out,
+                       gs_stream stream) {
+  if (!offsets || !out) return GS_ERROR_INVALID_ARGUMENT;
+  if (count && (!rows || !out->position || !out->cov3d || !out->opacity || !out->sh)) return GS_ERROR_INVALID_ARGUMENT;
+  if (offsets[59] == 0) return GS_ERROR_INVALID_ARGUMENT;
+  for (int i = 0; i < 59; ++i)
+    if (offsets[i] >= offsets[59]) return GS_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(out->sh) & 3u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  PlyOffsets off;
+  std::memcpy(off.v, offsets, sizeof(off.v));
+  return from_cuda(launch_parse_ply(rows, count, off, out->position, out->cov3d, out->opacity, out->sh,
+                                    reinterpret_cast<cudaStream_t>(stream)));
+}
+
+gs_status gs_ply_offsets_from_header(const char* text, size_t length, uint32_t offsets[60], uint64_t* point_count,
+                                     size_t* header_bytes) {
+  if (!text || !offsets || !point_count || !header_bytes) return GS_ERROR_INVALID_ARGUMENT;
+  struct Prop {
+    std::string name;
+    uint32_t offset;
+  };
+  Prop props[256];
+  int nprops = 0;
+  uint32_t offset = 0;
+  uint64_t count = 0;
+  bool in_vertex = false, saw_end = false, binary_le = false, magic = false;
+  size_t pos = 0;
+  int line_no = 0;
+  while (pos < length) {
+    size_t eol = pos;
+    while (eol < length && text[eol] != '\n') ++eol;
+    std::string line(text + pos, eol - pos);
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    pos = eol < length ? eol + 1 : eol;
+    if (line_no++ == 0) {
+      magic = line == "ply";
+      if (!magic) return GS_ERROR_INVALID_ARGUMENT;
+      continue;
+    }
+    if (line == "end_header") {
+      saw_end = true;
+      break;
+    }
+    char w0[64] = {0}, w1[64] = {0}, w2[128] = {0};
+    const int nw = std::sscanf(line.c_str(), "%63s %63s %127s", w0, w1, w2);
+    if (nw < 1) continue;
+    if (!std::strcmp(w0, "format")) {
+      binary_le = nw >= 2 && !std::strcmp(w1, "binary_little_endian");
+    } else if (!std::strcmp(w0, "element")) {
+      in_vertex = nw >= 3 && !std::strcmp(w1, "vertex");
+      if (in_vertex) count = std::strtoull(w2, nullptr, 10);
+    } else if (!std::strcmp(w0, "property") && in_vertex) {
+      if (nw < 3 || std::strcmp(w1, "float") != 0 || nprops >= 256) return GS_ERROR_INVALID_ARGUMENT;
+      props[nprops].name = w2;
+      props[nprops].offset = offset;
+      ++nprops;
+      offset += 1;
+    }
+  }
+  if (!saw_end || !binary_le || nprops == 0) return GS_ERROR_INVALID_ARGUMENT;
+  auto find = [&](const std::string& name, uint32_t* dst) {
+    for (int i = 0; i < nprops; ++i)
+      if (props[i].name == name) {
+        *dst = props[i].offset;
+        return true;
+      }
+    return false;
+  };
+  bool ok = find("x", &offsets[0]) && find("y", &offsets[1]) && find("z", &offsets[2]) &&
+            find("scale_0", &offsets[3]) && find("scale_1", &offsets[4]) && find("scale_2", &offsets[5]) &&
+            find("rot_1", &offsets[6]) && find("rot_2", &offsets[7]) && find("rot_3", &offsets[8]) &&
+            find("rot_0", &offsets[9]) && find("f_dc_0", &offsets[10]) && find("f_dc_1", &offsets[26]) &&
+            find("f_dc_2", &offsets[42]) && find("opacity", &offsets[58]);
+  for (int i = 0; ok && i < 15; ++i) {
+    ok = find("f_rest_" + std::to_string(i), &offsets[11 + i]) &&
+         find("f_rest_" + std::to_string(15 + i), &offsets[27 + i]) &&
+         find("f_rest_" + std::to_string(30 + i), &offsets[43 + i]);
+  }
+  if (!ok) return GS_ERROR_INVALID_ARGUMENT;
+  offsets[59] = offset;
+  *point_count = count;
+  *header_bytes = pos;
+  return GS_SUCCESS;
+}
+
+// ------------------------------------------------------------------ camera
+
+void gs_camera_perspective(float fovy, float aspect, float znear, float zfar, float out[16]) {
+  float p[16] = {0};
+  const float t = std::tan(fovy / 2.0f);
+  p[0] = 1.0f / (aspect * t);
+  p[5] = 1.0f / t;
+  p[10] = -(zfar + znear) / (zfar - znear);
+  p[11] = -1.0f;
+  p[14] = -(2.0f * zfar * znear) / (zfar - znear);
+  float conv[16] = {0};
+  conv[0] = 1.0f;
+  conv[5] = -1.0f;
+  conv[10] = 0.5f;
+  conv[14] = 0.5f;
+  conv[15] = 1.0f;
+  gs::mat4_mul_host(conv, p, out);
+}
+
+static float dot3(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static void normalize3(const float* v, float* o) {
+  const float inv = 1.0f / std::sqrt(dot3(v, v));
+  o[0] = v[0] * inv;
+  o[1] = v[1] * inv;
+  o[2] = v[2] * inv;
+}
+
+static void cross3(const float* a, const float* b, float* o) {
+  o[0] = a[1] * b[2] - b[1] * a[2];
+  o[1] = a[2] * b[0] - b[2] * a[0];
+  o[2] = a[0] * b[1] - b[0] * a[1];
+}
+
+void gs_camera_look_at(const float eye[3], const float center[3], const float up[3], float out[16]) {
+  const float d[3] = {center[0] - eye[0], center[1] - eye[1], center[2] - eye[2]};
+  float f[3], s[3], sn[3], u[3];
+  normalize3(d, f);
+  cross3(f, up, s);
+  normalize3(s, sn);
+  cross3(sn, f, u);
+  for (int i = 0; i < 16; ++i) out[i] = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    out[k * 4 + 0] = sn[k];
+    out[k * 4 + 1] = u[k];
+    out[k * 4 + 2] = -f[k];
+  }
+  out[12] = -dot3(sn, eye);
+  out[13] = -dot3(u, eye);
+  out[14] = dot3(f, eye);
+  out[15] = 1.0f;
+}
+
+void gs_camera_orbit_eye(const float center[3], float r, float phi, float theta, float out[3]) {
+  const float sp = std::sin(phi), cp = std::cos(phi), st = std::sin(theta), ct = std::cos(theta);
+  const float d[3] = {sp * st, cp, sp * ct};
+  for (int i = 0; i < 3; ++i) out[i] = center[i] + r * d[i];
+}
+
+}  // extern "C"

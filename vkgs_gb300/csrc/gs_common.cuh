@@ -1,0 +1,123 @@
+// gs_common.cuh -- device helpers shared by the splat pipeline kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gs {
+
+typedef uint32_t u32;
+typedef uint64_t u64;
+
+// Bits of the device error word (read back by gs_context_check / gs_sorter_check).
+enum : u32 {
+  ERR_CAPACITY = 1u,  // more (splat, tile) pairs than the context holds, or a sort count beyond max_count
+  ERR_TIMEOUT = 2u,   // a bounded look-back wait gave up
+};
+
+// Upper bound on polls of one look-back status word.  A predecessor partition publishes its
+// aggregate within microseconds of starting; a wait this long means it will never come, so the
+// waiter records ERR_TIMEOUT and carries on with a zero contribution instead of hanging the GPU.
+constexpr u32 kMaxSpins = 1u << 21;
+
+__device__ __forceinline__ u64 ld_relaxed_u64(const u64* p) {
+  u64 v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(u64* p, u64 v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ u32 lanemask_lt() {
+  u32 m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Decoupled look-back status word: [63:32] epoch, [31:30] flag, [29:0] value.  A word whose epoch
+// differs from the caller's is "not yet published" for this pass, so the status array never needs
+// clearing between passes or frames.
+enum : u32 { LB_AGGREGATE = 1u, LB_INCLUSIVE = 2u };
+
+__device__ __forceinline__ u64 lb_pack(u32 epoch, u32 flag, u32 value) {
+  return ((u64)epoch << 32) | ((u64)flag << 30) | (u64)(value & 0x3fffffffu);
+}
+
+// One thread's look-back for partition p over status words status[j * stride] (j < p).  Publishes
+// `aggregate`, walks back until an inclusive prefix is found, publishes its own inclusive prefix and
+// returns the exclusive prefix.  Every wait is bounded by kMaxSpins.
+__device__ __forceinline__ u32 lookback(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
+  u64* mine = status + (size_t)p * stride;
+  if (p == 0) {
+    st_relaxed_u64(mine, lb_pack(epoch, LB_INCLUSIVE, aggregate));
+    return 0;
+  }
+  st_relaxed_u64(mine, lb_pack(epoch, LB_AGGREGATE, aggregate));
+  u32 exclusive = 0;
+  int j = (int)p - 1;
+  u32 spins = 0;
+  while (j >= 0) {
+    const u64 s = ld_relaxed_u64(status + (size_t)j * stride);
+    const u32 flag = (u32)(s >> 30) & 3u;
+    if ((u32)(s >> 32) != epoch || flag == 0) {
+      if (++spins > kMaxSpins) {
+        atomicOr(err, ERR_TIMEOUT);
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    exclusive += (u32)s & 0x3fffffffu;
+    if (flag == LB_INCLUSIVE) break;
+    --j;
+  }
+  st_relaxed_u64(mine, lb_pack(epoch, LB_INCLUSIVE, exclusive + aggregate));
+  return exclusive;
+}
+
+// Exclusive scan of one value per thread across a block of NT threads (NT multiple of 32, <= 1024).
+// Returns the exclusive prefix; *total receives the block sum.  Contains __syncthreads.
+template <int NT>
+__device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp /* >= NT/32 words */, u32* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    u32 w = (lane < NT / 32) ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < NT / 32) s_warp[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  const u32 before = warp ? s_warp[warp - 1] : 0u;
+  *total = s_warp[NT / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// Per-frame constants of one camera (the Camera uniform + model push constant, pre-multiplied
+// where the reference multiplies per invocation).  Passed by value to the kernels.
+struct FrameConst {
+  float pvm[16];    // projection * view * model, glm operand order (rank.comp:32)
+  float model[16];
+  float view[16];
+  float proj[16];
+  float cam_m[3];   // inverse(model) * camera_position, divided by w (projection.comp:85-86)
+  float lpx, lpy;   // 1/W/W and 1/H/H (projection.comp:115-116)
+  u32 width, height;
+  u32 model_identity;
+  u32 n;
+};
+
+}  // namespace gs

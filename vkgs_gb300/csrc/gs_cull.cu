@@ -1,0 +1,279 @@
+// gs_cull.cu -- rank.comp + projection.comp fused into one pass over the splats in id order.
+//
+// Compiled with --fmad=false: every product and sum below is one IEEE binary32 rounding in the
+// operand order of the GLSL source (column-major matrices, left-to-right sums), so the visible set,
+// the keys and the projected records are bit-identical to the scalar restatement of the shaders.
+//
+// Per 1024-splat partition (partitions taken in ticket order by persistent CTAs):
+//   1. rank.comp:27-41 -- clip = (P*V*M) * pos, ndc = clip / clip.w, visible iff |x|<=1, |y|<=1,
+//      0<=z<=1, key = floatBitsToUint(1 - z);
+//   2. the reference's atomicAdd slot becomes an order-preserving compaction (ballot counts per warp,
+//      a bounded decoupled look-back across partitions), so equal keys later sort by ascending id;
+//   3. projection.comp:80-179 for every visible splat, written at record[id] (raster record) and,
+//      if requested, inst_by_id[id] (the reference's 48-byte instance layout).
+// The reference's inverse-index pass (inverse_index.comp) has no counterpart: records are keyed by
+// splat id and the later stages gather them through the sorted index list.
+#include <cuda_fp16.h>
+
+#include "gs_common.cuh"
+#include "gs_internal.h"
+
+namespace gs {
+
+__device__ __forceinline__ void mat4_vec4(const float* m, const float v[4], float out[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) out[i] = ((m[i] * v[0] + m[4 + i] * v[1]) + m[8 + i] * v[2]) + m[12 + i] * v[3];
+}
+
+// cov <- m3 * cov * transpose(m3), m3 = mat3(m4), evaluated as (m3 * cov) * m3^T, all 9 entries.
+__device__ __forceinline__ void sandwich3(const float* m4, float c[9]) {
+  float t[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      t[j * 3 + i] = (m4[0 * 4 + i] * c[j * 3 + 0] + m4[1 * 4 + i] * c[j * 3 + 1]) + m4[2 * 4 + i] * c[j * 3 + 2];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      c[j * 3 + i] = (t[0 * 3 + i] * m4[0 * 4 + j] + t[1 * 3 + i] * m4[1 * 4 + j]) + t[2 * 3 + i] * m4[2 * 4 + j];
+}
+
+__device__ __forceinline__ float dot4(float a0, float a1, float a2, float a3, float b0, float b1, float b2, float b3) {
+  return ((a0 * b0 + a1 * b1) + a2 * b2) + a3 * b3;
+}
+
+__device__ __forceinline__ void unpack_half8(const uint4 q, float f[8]) {
+  const __half2* h = reinterpret_cast<const __half2*>(&q);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 v = __half22float2(h[i]);
+    f[2 * i] = v.x;
+    f[2 * i + 1] = v.y;
+  }
+}
+
+__device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, float x0, float y0, float z0) {
+  // direction for SH in model space (projection.comp:85-87); normalize = v / sqrt(dot(v, v))
+  const float ddx = x0 - fc.cam_m[0], ddy = y0 - fc.cam_m[1], ddz = z0 - fc.cam_m[2];
+  const float dl = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
+  const float x = ddx / dl, y = ddy / dl, z = ddz / dl;
+
+  const float* cv = a.cov3d + 6 * (size_t)id;
+  const float c0 = __ldg(cv + 0), c1 = __ldg(cv + 1), c2 = __ldg(cv + 2), c3 = __ldg(cv + 3), c4 = __ldg(cv + 4),
+              c5 = __ldg(cv + 5);
+  float C[9] = {c0, c1, c2, c1, c3, c4, c2, c4, c5};  // mat3(v0, v0.y, v1.xy, v0.z, v1.yz)
+  float p4[4] = {x0, y0, z0, 1.0f};
+  if (!fc.model_identity) {
+    sandwich3(fc.model, C);
+    float t[4];
+    mat4_vec4(fc.model, p4, t);
+    p4[0] = t[0], p4[1] = t[1], p4[2] = t[2], p4[3] = t[3];
+  }
+  sandwich3(fc.view, C);
+  float pv[4];
+  mat4_vec4(fc.view, p4, pv);
+
+  // J (projection.comp:105-108); only its first two rows reach the 2x2 block, and the
+  // structural zeros J[1][0] = J[0][1] = 0 contribute exact zeros to every sum they enter.
+  const float j00 = -1.0f / pv[2];
+  const float j20 = pv[0] / pv[2] / pv[2];
+  const float j21 = pv[1] / pv[2] / pv[2];
+  float jc0[3], jc1[3];  // (J * C)[k][0], (J * C)[k][1]
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    jc0[k] = j00 * C[k * 3 + 0] + j20 * C[k * 3 + 2];
+    jc1[k] = j00 * C[k * 3 + 1] + j21 * C[k * 3 + 2];
+  }
+  const float r00 = jc0[0] * j00 + jc0[2] * j20;  // (J C J^T)[0][0]
+  const float r01 = jc1[0] * j00 + jc1[2] * j20;  // [0][1]
+  const float r10 = jc0[1] * j00 + jc0[2] * j21;  // [1][0]
+  const float r11 = jc1[1] * j00 + jc1[2] * j21;  // [1][1]
+
+  // cov2d = mat2(P) * mat2(cov) * mat2(P) (projection.comp:111-112)
+  const float p00 = fc.proj[0], p01 = fc.proj[1], p10 = fc.proj[4], p11 = fc.proj[5];
+  const float t00 = p00 * r00 + p10 * r01, t01 = p01 * r00 + p11 * r01;
+  const float t10 = p00 * r10 + p10 * r11, t11 = p01 * r10 + p11 * r11;
+  const float a2 = (t00 * p00 + t10 * p01) + fc.lpx;
+  const float b2 = (t01 * p10 + t11 * p11) + fc.lpy;
+  const float c2d = t00 * p10 + t10 * p11;
+
+  // eigen decomposition (projection.comp:121-134); the angle through the half-angle identities
+  const float D = sqrtf((a2 - b2) * (a2 - b2) + 4.0f * c2d * c2d);
+  const float s0 = sqrtf(0.5f * (a2 + b2 + D));
+  const float s1 = sqrtf(0.5f * (a2 + b2 - D));
+  const float sin2t = 2.0f * c2d / D;
+  const float cos2t = (a2 - b2) / D;
+  float ct, st;
+  if (cos2t >= 0.0f) {
+    ct = sqrtf(0.5f * (1.0f + cos2t));
+    st = sin2t / (2.0f * ct);
+  } else {
+    const float s = sqrtf(0.5f * (1.0f - cos2t));
+    st = copysignf(s, sin2t);
+    ct = fabsf(sin2t) / (2.0f * s);
+  }
+  const float rs0 = s0 * ct, rs1 = s0 * st, rs2 = -s1 * st, rs3 = s1 * ct;
+
+  // ndc (projection.comp:136-137)
+  float pc[4];
+  mat4_vec4(fc.proj, pv, pc);
+  const float nx = pc[0] / pc[3], ny = pc[1] / pc[3], nz = pc[2] / pc[3];
+
+  // SH degree 3 (projection.comp:140-174)
+  const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f, C20 = 1.0925484305920792f,
+              C21 = 0.31539156525252005f, C22 = 0.5462742152960396f, C30 = 0.5900435899266435f,
+              C31 = 2.890611442640554f, C32 = 0.4570457994644658f, C33 = 0.3731763325901154f,
+              C34 = 1.445305721320277f;
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  const float b00 = C0, b01 = -C1 * y, b02 = C1 * z, b03 = -C1 * x;
+  const float b10 = C20 * xy, b11 = -C20 * yz, b12 = C21 * (2.0f * zz - xx - yy), b13 = -C20 * xz;
+  const float b20 = C22 * (xx - yy), b21 = -C30 * y * (3.0f * xx - yy), b22 = C31 * xy * z,
+              b23 = -C32 * y * (4.0f * zz - xx - yy);
+  const float b30 = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), b31 = -C32 * x * (4.0f * zz - xx - yy),
+              b32 = C34 * z * (xx - yy), b33 = -C30 * x * (xx - 3.0f * yy);
+  const uint4* shv = reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)id);
+  float color[3];
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    float g[16];
+    unpack_half8(__ldg(shv + 2 * ch), g);
+    unpack_half8(__ldg(shv + 2 * ch + 1), g + 8);
+    const float col = ((dot4(b00, b01, b02, b03, g[0], g[1], g[2], g[3]) +
+                        dot4(b10, b11, b12, b13, g[4], g[5], g[6], g[7])) +
+                       dot4(b20, b21, b22, b23, g[8], g[9], g[10], g[11])) +
+                      dot4(b30, b31, b32, b33, g[12], g[13], g[14], g[15]);
+    color[ch] = fmaxf(col + 0.5f, 0.0f);
+  }
+  const float o = __ldg(a.opacity + id);
+
+  const float m00 = ct / s0, m01 = st / s0, m10 = -st / s1, m11 = ct / s1;
+  const bool drawn = (s1 > 0.0f) && isfinite(m00) && isfinite(m01) && isfinite(m10) && isfinite(m11) &&
+                     (nz >= 0.0f) && (nz < 1.0f);
+  float4* rec = a.record + 4 * (size_t)id;
+  rec[0] = make_float4(nx, ny, m00, m01);
+  rec[1] = make_float4(m10, m11, nz, o);
+  rec[2] = make_float4(fminf(color[0], 1.0f), fminf(color[1], 1.0f), fminf(color[2], 1.0f), 0.0f);
+  rec[3] = drawn ? make_float4(3.0f * (fabsf(rs0) + fabsf(rs2)), 3.0f * (fabsf(rs1) + fabsf(rs3)), 0.0f, 0.0f)
+                 : make_float4(-1.0f, -1.0f, 0.0f, 0.0f);
+  if (a.inst_by_id) {
+    float4* inst = reinterpret_cast<float4*>(a.inst_by_id + 12 * (size_t)id);
+    inst[0] = make_float4(nx, ny, nz, 0.0f);
+    inst[1] = make_float4(rs0, rs1, rs2, rs3);
+    inst[2] = make_float4(color[0], color[1], color[2], o);
+  }
+}
+
+__global__ __launch_bounds__(kCullThreads) void k_cull_project(const FrameConst fc, const CullArgs a) {
+  __shared__ u32 s_cnt[kCullItems][kCullThreads / 32];
+  __shared__ u32 s_off[kCullItems][kCullThreads / 32];
+  __shared__ u32 s_base;
+  __shared__ u32 s_part;
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const u32 n = fc.n;
+  const u32 nparts = (n + kCullTile - 1) / kCullTile;
+  const u32 lt = lanemask_lt();
+  for (;;) {
+    if (tid == 0) s_part = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    const u32 p = s_part;
+    if (p >= nparts) break;
+    float px[kCullItems], py[kCullItems], pz[kCullItems];
+    u32 key[kCullItems], ball[kCullItems];
+    bool vis[kCullItems];
+#pragma unroll
+    for (u32 k = 0; k < kCullItems; ++k) {
+      const u32 id = p * kCullTile + k * kCullThreads + tid;
+      vis[k] = false;
+      key[k] = 0;
+      px[k] = py[k] = pz[k] = 0.0f;
+      if (id < n) {
+        px[k] = __ldg(a.position + 3 * (size_t)id + 0);
+        py[k] = __ldg(a.position + 3 * (size_t)id + 1);
+        pz[k] = __ldg(a.position + 3 * (size_t)id + 2);
+        const float v[4] = {px[k], py[k], pz[k], 1.0f};
+        float c[4];
+        mat4_vec4(fc.pvm, v, c);
+        const float x = c[0] / c[3], y = c[1] / c[3], z = c[2] / c[3];
+        vis[k] = fabsf(x) <= 1.0f && fabsf(y) <= 1.0f && z >= 0.0f && z <= 1.0f;
+        key[k] = __float_as_uint(1.0f - z);
+      }
+      ball[k] = __ballot_sync(0xffffffffu, vis[k]);
+      if (lane == 0) s_cnt[k][warp] = __popc(ball[k]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      u32 acc = 0;
+      for (u32 k = 0; k < kCullItems; ++k)
+        for (u32 w = 0; w < kCullThreads / 32; ++w) {
+          s_off[k][w] = acc;
+          acc += s_cnt[k][w];
+        }
+      const u32 excl = lookback(a.status, 1, p, a.epoch, acc, a.err);
+      s_base = excl;
+      if (p == nparts - 1) *a.visible_count = excl + acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (u32 k = 0; k < kCullItems; ++k) {
+      if (vis[k]) {
+        const u32 id = p * kCullTile + k * kCullThreads + tid;
+        const u32 slot = s_base + s_off[k][warp] + __popc(ball[k] & lt);
+        a.key[slot] = key[k];
+        a.index[slot] = id;
+      }
+    }
+#pragma unroll 1
+    for (u32 k = 0; k < kCullItems; ++k)
+      if (vis[k]) project_splat(fc, a, p * kCullTile + k * kCullThreads + tid, px[k], py[k], pz[k]);
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream) {
+  if (fc.n == 0) return cudaSuccess;
+  const u32 parts = (fc.n + kCullTile - 1) / kCullTile;
+  const int sms = a.num_sms > 0 ? a.num_sms : 1;
+  const u32 grid = min(parts, (u32)sms * 8u);
+  k_cull_project<<<grid, kCullThreads, 0, stream>>>(fc, a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Instance records in sorted order + indirect draw arguments (projection.comp:64-75, 177-179).
+
+__global__ void k_instances(const u32* __restrict__ index, const u32* __restrict__ visible_count,
+                            const float4* __restrict__ inst_by_id, u32 n, float4* __restrict__ instances,
+                            u32* __restrict__ draw) {
+  const u32 v = min(*visible_count, n);
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 r = blockIdx.x * blockDim.x + threadIdx.x; instances && r < v; r += stride) {
+    const u32 id = index[r];
+    instances[3 * (size_t)r + 0] = inst_by_id[3 * (size_t)id + 0];
+    instances[3 * (size_t)r + 1] = inst_by_id[3 * (size_t)id + 1];
+    instances[3 * (size_t)r + 2] = inst_by_id[3 * (size_t)id + 2];
+  }
+  if (draw && blockIdx.x == 0 && threadIdx.x == 0) {
+    draw[0] = 6 * v;  // indexCount
+    draw[1] = 1;      // instanceCount
+    draw[2] = 0;      // firstIndex
+    draw[3] = 0;      // vertexOffset
+    draw[4] = 0;      // firstInstance
+    draw[5] = draw[6] = draw[7] = 0;
+    draw[8] = v;      // vertexCount of the point-list draw
+    draw[9] = 1;
+    draw[10] = 0;
+    draw[11] = 0;
+  }
+}
+
+cudaError_t launch_instances(const u32* index, const u32* visible_count, const float* inst_by_id, u32 n,
+                             float* instances, u32* draw_indirect, cudaStream_t stream) {
+  const u32 grid = max(1u, min((n + 255) / 256, 4096u));
+  k_instances<<<grid, 256, 0, stream>>>(index, visible_count, reinterpret_cast<const float4*>(inst_by_id), n,
+                                        reinterpret_cast<float4*>(instances), draw_indirect);
+  return cudaGetLastError();
+}
+
+}  // namespace gs

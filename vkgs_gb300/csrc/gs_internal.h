@@ -1,0 +1,115 @@
+// gs_internal.h -- host-side declarations shared by the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "gs_common.cuh"
+
+namespace gs {
+
+// ---- radix sort (gs_sort.cu) ----
+constexpr size_t kRadixControlBytes = (4 * 256 + 4) * sizeof(uint32_t);
+
+struct RadixSortArgs {
+  u32* keys;          // in/out (even pass count) -- see radix_sort
+  u32* values;        // may be null
+  u32* keys_alt;      // ping-pong buffers, max_count words
+  u32* values_alt;
+  const u32* count;   // device word
+  u32 max_count;
+  u32 begin_bit, end_bit;
+  u32* control;       // kRadixControlBytes, cleared by radix_sort
+  u64* status;        // radix_status_words(max_count) words, epoch-tagged
+  u32 epoch;          // first epoch; passes use epoch .. epoch + passes - 1 (never 0)
+  u32* err;           // device error word
+  int num_sms;
+};
+
+u32 radix_passes(u32 begin_bit, u32 end_bit);
+size_t radix_status_words(u32 max_count);
+// Sorts keys[0..*count) (and values) on bits [begin_bit, end_bit).  After an odd number of passes the
+// result lies in keys_alt / values_alt.
+cudaError_t radix_sort(const RadixSortArgs& a, cudaStream_t stream);
+
+// ---- cull + key + compaction + projection (gs_cull.cu) ----
+constexpr u32 kCullThreads = 256;
+constexpr u32 kCullItems = 4;
+constexpr u32 kCullTile = kCullThreads * kCullItems;
+
+struct CullArgs {
+  const float* position;
+  const float* cov3d;
+  const float* opacity;
+  const uint16_t* sh;
+  u32* key;          // compacted keys, ascending id
+  u32* index;        // compacted ids
+  float4* record;    // N x 4 float4 raster records, indexed by id
+  float* inst_by_id; // optional N x 12 reference instance records, indexed by id
+  u32* visible_count;
+  u64* status;       // >= ceil(N / kCullTile) words
+  u32* ticket;
+  u32 epoch;
+  u32* err;
+  int num_sms;
+};
+cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
+
+// Gathers instance records into sorted order and writes the indirect draw arguments.
+cudaError_t launch_instances(const u32* index, const u32* visible_count, const float* inst_by_id, u32 n,
+                             float* instances, u32* draw_indirect, cudaStream_t stream);
+
+// ---- tile binning (gs_bin.cu) ----
+constexpr u32 kTile = 16;  // tile edge in pixels
+constexpr u32 kBinThreads = 256;
+constexpr u32 kBinItems = 4;
+constexpr u32 kBinTile = kBinThreads * kBinItems;
+
+struct BinArgs {
+  const u32* index;          // sorted splat ids
+  const u32* visible_count;
+  const float4* record;
+  u32 n;                     // launch bound for V
+  u32 width, height, tiles_x, tiles_y;
+  u32* pair_tile;            // out: tile id per pair
+  u32* pair_splat;           // out: splat id per pair
+  u32 pair_capacity;
+  u32* pair_count;           // out: min(total, capacity)
+  u32* pair_total;           // out: pairs needed
+  u64* status;
+  u32* ticket;
+  u32 epoch;
+  u32* err;
+  int num_sms;
+};
+cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream);
+cudaError_t launch_tile_ranges(const u32* pair_tile, const u32* pair_count, u32 capacity, u32* tile_range /*2*T*/,
+                               int num_sms, cudaStream_t stream);
+
+// ---- raster (gs_raster.cu) ----
+struct RasterArgs {
+  const u32* tile_range;     // [T][2] = (begin, end)
+  const u32* pair_splat;
+  const float4* record;
+  u32 width, height, tiles_x, tiles_y;
+  float* out_rgba;           // may be null
+  uchar4* out_bgra;          // may be null
+  const float* depth;        // may be null
+  float t_floor;             // blending stops once every pixel of a tile is below this transmittance
+  unsigned long long* fragments;  // non-null: count fragments (disables the early stop)
+};
+cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
+
+// ---- loader (gs_ply.cu) ----
+struct PlyOffsets {
+  u32 v[60];
+};
+cudaError_t launch_parse_ply(const float* rows, u32 count, const PlyOffsets& off, float* position, float* cov3d,
+                             float* opacity, uint16_t* sh, cudaStream_t stream);
+
+// ---- camera constants (gs_api.cu) ----
+void frame_constants(const float projection[16], const float view[16], const float model[16], const float eye[3],
+                     u32 width, u32 height, u32 n, FrameConst* out);
+
+}  // namespace gs
