@@ -225,7 +225,11 @@ def test_parse_ply_on_gpu(cuda, oracle):
     pos, cov, opa, sh = oracle.parse_ply(rows, off)
     np.testing.assert_array_equal(sp.position.cpu().numpy(), pos)
     np.testing.assert_array_equal(sp.sh.cpu().numpy().view(np.uint16), sh)
-    np.testing.assert_allclose(sp.cov3d.cpu().numpy(), cov, rtol=2e-6, atol=1e-12)
+    # exp() may differ by an ulp between CUDA and libm; off-diagonal terms cancel, so bound the
+    # error relative to each splat's largest variance rather than to the entry itself.
+    got = sp.cov3d.cpu().numpy().astype(np.float64)
+    scale = np.abs(cov[:, [0, 3, 5]]).max(axis=1, keepdims=True).astype(np.float64)
+    assert (np.abs(got - cov) <= 4e-6 * scale).all()
     np.testing.assert_allclose(sp.opacity.cpu().numpy(), opa, rtol=1e-6)
 
 
