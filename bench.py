@@ -290,7 +290,7 @@ def run_ours(args):
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_peak = sms * 128 * sm_max * 1e6 / 1e12  # T lane-ops/s
     cam_of = [k % len(cams) for k in range(K)]
-    frags = np.array([stats[c]["fragments"] for c in cam_of], np.float64)
+    frags = np.array([stats[c]["fragments_blended"] for c in cam_of], np.float64)
     vis = np.array([stats[c]["visible_count"] for c in cam_of], np.float64)
     raster_ms = stage[:, 5].astype(np.float64)
     achieved = float((frags * OPS_PER_FRAGMENT).sum() / (raster_ms.sum() / 1e3) / 1e12)
@@ -335,17 +335,20 @@ def run_ours(args):
         "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
                      "unit": "T lane-ops/s", "frac": achieved / fp32_peak, "traffic": profile_traffic(),
                      "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
-                     "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair"},
+                     "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair met front to "
+                             "back while the pixel's transmittance is >= 2^-24"},
         "roofline_hbm": {**hbm_stages, "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "stages_ms": stage_mean,
         "dominant_stage": dominant,
         "frame_stats": {"visible": [s["visible_count"] for s in stats], "tile_pairs": [s["tile_pairs"] for s in stats],
-                        "fragments": [s["fragments"] for s in stats]},
+                        "fragments": [s["fragments"] for s in stats],
+                        "fragments_blended": [s["fragments_blended"] for s in stats]},
         "cpu_baseline": cpu,
         "clocks": clk,
     }
-    # cull_project, depth sort (histogram + 4 passes), bin, tile sort (histogram + 2 passes), ranges, raster
-    launches_per_frame = 1 + 5 + 1 + 3 + 1 + 1
+    # cull_project, depth sort (histogram + 4 passes), binning (count, reduce, block scan, scan, emit),
+    # tile sort (histogram + 2 passes), tile ranges, raster
+    launches_per_frame = 1 + 5 + 5 + 3 + 1 + 1
     line["gpu_launches"] = launches_per_frame * K
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -44,6 +44,7 @@ typedef enum gs_status {
   GS_ERROR_CUDA = 3,             /* a CUDA runtime call or kernel launch failed */
   GS_ERROR_DEVICE_TIMEOUT = 4,   /* a bounded device-side wait gave up (results of that call are invalid) */
   GS_ERROR_OUT_OF_MEMORY = 5,    /* device allocation failed while reserving */
+  GS_ERROR_INTERNAL = 6,         /* a device-side self-check failed (results of that call are invalid) */
 } gs_status;
 
 /* Short text for a status code (static storage). */
@@ -140,9 +141,13 @@ typedef struct gs_context_options {
 } gs_context_options;
 
 typedef struct gs_frame_stats {
-  uint32_t visible_count;   /* V of the last frame */
-  uint32_t tile_pairs;      /* (splat, tile) pairs the last frame needed */
-  uint64_t fragments;       /* covered (pixel, splat) pairs, only with gs_context_set_count_fragments(1) */
+  uint32_t visible_count;     /* V of the last frame */
+  uint32_t tile_pairs;        /* (splat, tile) pairs the last frame needed */
+  uint64_t fragments;         /* covered (pixel, splat) pairs passing the depth test: the fragment-shader
+                                 invocations of the reference's draw; only with
+                                 gs_context_set_count_fragments(1) */
+  uint64_t fragments_blended; /* of those, the ones met front to back while the pixel's transmittance
+                                 was still >= 2^-24 (the blend work actually needed) */
 } gs_frame_stats;
 
 /* Creates a context on the current CUDA device and reserves all scratch for the given capacities. */
@@ -163,7 +168,7 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,
- * tile binning, tile sort, tile ranges, raster + blend. */
+ * (splat, tile) pair count/scan/emission, stable tile sort of the pairs, tile ranges, raster + blend. */
 #define GS_NUM_STAGES 6
 gs_status gs_context_enable_timing(gs_context* context, int enable);
 

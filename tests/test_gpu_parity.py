@@ -280,14 +280,30 @@ def test_sorter_count_beyond_capacity_is_reported(cuda):
     assert np.all(k[:-1] <= k[1:])  # clamped to max_count and still sorted
 
 
-@pytest.mark.parametrize("cam_index", [0, 8])
-def test_large_workload_parity(cuda, oracle, cam_index):
-    """6M splats (shell layout), one circle camera and the zoomed-out camera, at full size."""
+@pytest.fixture(scope="module")
+def large_scene(oracle):
     rows = syn.splat_rows(6_000_000, 1, "shell")
-    act = scenes.activated(oracle, rows)
-    del rows
+    return scenes.activated(oracle, rows)
+
+
+@pytest.mark.parametrize("cam_index", [0, 1, 3, 8])
+def test_large_workload_parity(cuda, oracle, large_scene, cam_index):
+    """6M splats (shell layout) at 1600x900: circle cameras and the zoomed-out camera, at full size."""
     spec = syn.circle_cameras()[cam_index]
     c = scenes.camera(oracle, spec.eye, width=spec.width, height=spec.height)
-    g = render_gpu(act, c)
-    o = render_cpu(oracle, act, c)
+    g = render_gpu(large_scene, c)
+    o = render_cpu(oracle, large_scene, c)
     assert_parity(g, o)
+
+
+def test_many_random_cameras(cuda, oracle):
+    """500k splats, 12 random cameras of mixed resolution through one renderer."""
+    from vkgs_gb300 import Renderer
+
+    rows = syn.splat_rows(500_000, 21)
+    act = scenes.activated(oracle, rows)
+    specs = syn.random_cameras(12, seed=77)
+    r = Renderer(500_000, 1920, 1080)
+    for spec in specs:
+        c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=spec.width, height=spec.height)
+        assert_parity(render_gpu(act, c, renderer=r), render_cpu(oracle, act, c))

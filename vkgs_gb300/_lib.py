@@ -18,6 +18,7 @@ GS_ERROR_CAPACITY = 2
 GS_ERROR_CUDA = 3
 GS_ERROR_DEVICE_TIMEOUT = 4
 GS_ERROR_OUT_OF_MEMORY = 5
+GS_ERROR_INTERNAL = 6
 GS_NUM_STAGES = 6
 STAGES = ("cull_project", "depth_sort", "bin", "tile_sort", "tile_ranges", "raster")
 
@@ -51,7 +52,8 @@ class GsContextOptions(ctypes.Structure):
 
 
 class GsFrameStats(ctypes.Structure):
-    _fields_ = [("visible_count", c_uint32), ("tile_pairs", c_uint32), ("fragments", c_uint64)]
+    _fields_ = [("visible_count", c_uint32), ("tile_pairs", c_uint32), ("fragments", c_uint64),
+                ("fragments_blended", c_uint64)]
 
 
 # (name, restype, argtypes) for every entry point of include/vkgs_gb300.h

@@ -242,7 +242,7 @@ class Renderer:
         st = L.GsFrameStats()
         status = self._lib.gs_context_check(self._h, _stream(stream), ctypes.byref(st))
         stats = {"visible_count": int(st.visible_count), "tile_pairs": int(st.tile_pairs),
-                 "fragments": int(st.fragments)}
+                 "fragments": int(st.fragments), "fragments_blended": int(st.fragments_blended)}
         if status != L.GS_SUCCESS:
             err = GsError(status, "gs_context_check")
             err.stats = stats

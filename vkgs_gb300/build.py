@@ -29,7 +29,8 @@ UNITS = {
     "gs_cull.cu": ["--fmad=false"],
     "gs_ply.cu": ["--fmad=false"],
     "gs_sort.cu": [],
-    "gs_bin.cu": [],
+    # the count and emit kernels evaluate the same tile-footprint arithmetic and must agree exactly
+    "gs_bin.cu": ["--fmad=false"],
     "gs_raster.cu": ["-ftz=true"],
 }
 HEADERS = ["gs_common.cuh", "gs_internal.h"]

@@ -43,12 +43,6 @@ struct Carver {
   }
 };
 
-u32 ceil_log2(u32 x) {
-  u32 b = 0;
-  while (b < 32 && (1ull << b) < x) ++b;
-  return b;
-}
-
 gs_status from_cuda(cudaError_t e) { return e == cudaSuccess ? GS_SUCCESS : GS_ERROR_CUDA; }
 
 // Frame-local device words (cleared at the start of every frame).
@@ -57,8 +51,7 @@ enum FrameWord : u32 {
   FW_PAIR_COUNT = 1,
   FW_PAIR_TOTAL = 2,
   FW_TICKET_CULL = 3,
-  FW_TICKET_BIN = 4,
-  FW_FRAGMENTS = 6,  // u64 at words 6..7
+  FW_FRAGMENTS = 4,  // u64 covered fragments at words 4..5, u64 blended fragments at 6..7
   FW_WORDS = 16,
 };
 
@@ -82,10 +75,11 @@ struct gs_context {
   float4* record = nullptr;
   float* inst_by_id = nullptr;
   u64* cull_status = nullptr;
-  u64* bin_status = nullptr;
   u32* radix_control = nullptr;
   u64* radix_status = nullptr;
   size_t radix_status_words = 0;
+  u32* bin_count = nullptr;
+  u32* bin_block_sum = nullptr;
   u32* pair_tile = nullptr;
   u32* pair_splat = nullptr;
   u32* pair_tile_alt = nullptr;
@@ -122,6 +116,7 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
   const u32 max_tiles = std::max(1u, tiles_x * tiles_y);
   const u32 n = std::max(1u, max_splats);
   const u32 pairs = std::max(1u, max_pairs);
+  if (max_tiles > kMaxTiles) return GS_ERROR_CAPACITY;
   Carver plan;
   auto layout = [&](Carver& cv, gs_context* t) {
     t->frame = cv.take<u32>(FW_WORDS);
@@ -132,6 +127,8 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->index_alt = cv.take<u32>(n);
     t->record = cv.take<float4>((size_t)n * 4);
     t->inst_by_id = cv.take<float>((size_t)n * 12);
+    t->bin_count = cv.take<u32>(n);
+    t->bin_block_sum = cv.take<u32>(bin_block_sums(n));
     t->tile_range = cv.take<u32>((size_t)max_tiles * 2);
     t->radix_control = cv.take<u32>(kRadixControlBytes / sizeof(u32));
     t->pair_tile = cv.take<u32>(pairs);
@@ -140,7 +137,6 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->pair_splat_alt = cv.take<u32>(pairs);
     t->status_bytes_begin = cv.offset;
     t->cull_status = cv.take<u64>((n + kCullTile - 1) / kCullTile);
-    t->bin_status = cv.take<u64>((n + kBinTile - 1) / kBinTile);
     t->radix_status_words = radix_status_words(std::max(n, pairs));
     t->radix_status = cv.take<u64>(t->radix_status_words);
     t->status_bytes_end = cv.offset;
@@ -250,6 +246,7 @@ const char* gs_status_string(gs_status s) {
     case GS_ERROR_CUDA: return "CUDA error";
     case GS_ERROR_DEVICE_TIMEOUT: return "device-side wait timed out";
     case GS_ERROR_OUT_OF_MEMORY: return "out of device memory";
+    case GS_ERROR_INTERNAL: return "device-side self-check failed";
   }
   return "unknown status";
 }
@@ -334,6 +331,7 @@ gs_status gs_sorter_check(gs_sorter* s, gs_stream stream) {
   if (cudaMemcpy(&e, s->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return GS_ERROR_CUDA;
   cudaMemset(s->err, 0, 4);
   if (e & ERR_TIMEOUT) return GS_ERROR_DEVICE_TIMEOUT;
+  if (e & ERR_INTERNAL) return GS_ERROR_INTERNAL;
   if (e & ERR_CAPACITY) return GS_ERROR_CAPACITY;
   return GS_SUCCESS;
 }
@@ -516,22 +514,22 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   ba.height = H;
   ba.tiles_x = tiles_x;
   ba.tiles_y = tiles_y;
+  ba.count = c->bin_count;
+  ba.block_sum = c->bin_block_sum;
   ba.pair_tile = c->pair_tile;
   ba.pair_splat = c->pair_splat;
   ba.pair_capacity = c->pair_capacity;
   ba.pair_count = c->frame + FW_PAIR_COUNT;
   ba.pair_total = c->frame + FW_PAIR_TOTAL;
-  ba.status = c->bin_status;
-  ba.ticket = c->frame + FW_TICKET_BIN;
-  ba.epoch = c->take_epochs(1);
   ba.err = c->err;
-  ba.num_sms = c->num_sms;
-  GS_TRY(launch_bin(ba, st));
+  GS_TRY(launch_bin(ba, st, nullptr, nullptr, c->num_sms));
   GS_MARK(3);
 
+  // Stable sort of the pairs by tile id alone: each tile's list keeps the sorted (draw) order.
   const u32* sorted_tile = c->pair_tile;
   const u32* sorted_splat = c->pair_splat;
-  const u32 tile_bits = ceil_log2(tiles);
+  u32 tile_bits = 0;
+  while (tile_bits < 32 && (1ull << tile_bits) < tiles) ++tile_bits;
   if (n > 0 && tile_bits > 0) {
     RadixSortArgs ra{};
     ra.keys = c->pair_tile;
@@ -555,11 +553,12 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     }
   }
   GS_MARK(4);
-  if (n > 0) GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range,
-                                       c->num_sms, st));
+  if (n > 0)
+    GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range, c->num_sms, st));
 
   RasterArgs rr{};
   rr.tile_range = c->tile_range;
+  rr.pair_capacity = c->pair_capacity;
   rr.pair_splat = sorted_splat;
   rr.record = c->record;
   rr.width = W;
@@ -594,11 +593,13 @@ gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stat
   if (stats) {
     stats->visible_count = words[FW_VISIBLE];
     stats->tile_pairs = words[FW_PAIR_TOTAL];
-    uint64_t f;
-    std::memcpy(&f, words + FW_FRAGMENTS, 8);
-    stats->fragments = f;
+    uint64_t f[2];
+    std::memcpy(f, words + FW_FRAGMENTS, 16);
+    stats->fragments = f[0];
+    stats->fragments_blended = f[1];
   }
   if (e & ERR_TIMEOUT) return GS_ERROR_DEVICE_TIMEOUT;
+  if (e & ERR_INTERNAL) return GS_ERROR_INTERNAL;
   if (e & ERR_CAPACITY) return GS_ERROR_CAPACITY;
   return GS_SUCCESS;
 }

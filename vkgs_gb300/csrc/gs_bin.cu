@@ -1,146 +1,289 @@
-// gs_bin.cu -- (splat, tile) pairs in sorted order, then per-tile ranges after the tile sort.
+// gs_bin.cu -- (splat, tile) pairs in draw order, grouped by tile.
 //
-// The reference rasterises one quad per sorted splat with the fixed-function pipeline
-// (splat.vert:10-25, engine.cc:1474-1479).  Here every visible splat is listed in each 16x16 tile
-// its 3-sigma quad can cover.  Pairs are emitted in ascending sorted position, so a stable sort on
-// the tile id alone leaves every tile's list in the reference's draw order.
-//
-// Tile test: the tile's pixel-centre rectangle against the quad.  The rectangle's axes are covered by
-// the quad's bounding box (the tile range); the quad's own axes by mapping the rectangle into the
-// quad's unit frame p = rot_scale^-1 (x - c) and testing the p-range against [-3, 3].  Both tests are
-// conservative (one pixel / a relative margin), so no pixel the rasteriser covers is ever dropped.
+// The reference draws one quad per sorted splat with the fixed-function rasteriser
+// (splat.vert:10-25, engine.cc:1474-1479); the blend order of every pixel is the sorted order.  Here
+// each 16x16 tile receives the list of splats whose 3-sigma quad can cover one of its pixel centres:
+//   1. count : per sorted splat, the number of tiles its quad reaches -> count[r]
+//   2. scan  : exclusive scan of count[] -> first[r] and the pair total P (reduce-then-scan, no waits)
+//   3. emit  : each warp expands the pairs of 32 consecutive sorted splats in order into shared memory
+//              and stores them coalesced at [first[r0], ...): pairs leave in ascending sorted position
+//   4. a stable radix sort on the tile id alone (gs_sort.cu) then groups them by tile without
+//      disturbing that order, and tile ranges are read off the sorted tile ids.
+// The tile test is exact up to a small margin: the quad (corners c +- a +- b) is clipped to each tile
+// row's band of pixel centres and the tile columns its x-extent reaches are taken; the margin only
+// ever adds pairs.  count and emit evaluate the same footprint arithmetic (this unit is compiled
+// without FMA contraction) and emit checks that every splat produced exactly its counted pairs.
 #include "gs_common.cuh"
 #include "gs_internal.h"
 
 namespace gs {
 
-struct TileRect {
-  int tx0, tx1, ty0, ty1;  // inclusive; tx0 > tx1 when empty
+constexpr u32 kCountThreads = 256;
+constexpr u32 kEmitThreads = 256;
+constexpr u32 kEmitWarps = kEmitThreads / 32;
+constexpr u32 kEmitBuf = 512;       // expanded pairs per warp and window
+constexpr u32 kScanThreads = 256;
+constexpr u32 kScanItems = 16;
+constexpr u32 kScanTile = kScanThreads * kScanItems;  // counts per scan block
+constexpr float kMarginPx = 0.25f;
+
+// The quad of one splat prepared for row clipping: corners in order and inverse edge slopes.
+struct Footprint {
+  float vx[4], vy[4], dxdy[4];
+  int ty0, ty1;  // tile rows it may reach (empty when ty0 > ty1)
 };
 
-__device__ __forceinline__ float pixel_ndc(int i, u32 size) { return (float)(2 * i + 1) / (float)size - 1.0f; }
+struct TargetGeom {
+  u32 width, height, tiles_x;
+  float inv_w, inv_h;  // 1/W, 1/H
+};
 
-// Inclusive pixel range whose centres may lie within [c - h, c + h] (NDC), padded by one pixel.
-__device__ __forceinline__ void pixel_span(float c, float h, u32 size, int* lo, int* hi) {
-  float a = ((c - h + 1.0f) * (float)size - 1.0f) * 0.5f;
-  float b = ((c + h + 1.0f) * (float)size - 1.0f) * 0.5f;
-  a = fminf(fmaxf(floorf(a) - 1.0f, -1.0f), (float)size);
-  b = fmaxf(fminf(ceilf(b) + 1.0f, (float)size), -1.0f);
-  *lo = (int)a < 0 ? 0 : (int)a;
-  *hi = (int)b > (int)size - 1 ? (int)size - 1 : (int)b;
+__device__ __forceinline__ TargetGeom target_geom(const BinArgs& a) {
+  return TargetGeom{a.width, a.height, a.tiles_x, 1.0f / (float)a.width, 1.0f / (float)a.height};
 }
 
-__device__ __forceinline__ TileRect tile_rect(float4 q0, float4 q3, u32 width, u32 height) {
-  TileRect r{0, -1, 0, -1};
-  if (!(q3.x >= 0.0f)) return r;  // not drawn
-  int x0, x1, y0, y1;
-  pixel_span(q0.x, q3.x, width, &x0, &x1);
-  pixel_span(q0.y, q3.y, height, &y0, &y1);
-  if (x0 > x1 || y0 > y1) return r;
-  r.tx0 = x0 / (int)kTile;
-  r.tx1 = x1 / (int)kTile;
-  r.ty0 = y0 / (int)kTile;
-  r.ty1 = y1 / (int)kTile;
-  return r;
+// Inclusive range of pixel indices whose centres (2i+1)/size - 1 lie in [lo, hi] (NDC), clamped.
+__device__ __forceinline__ void pixel_range(float lo, float hi, u32 size, int& i0, int& i1) {
+  const float s = (float)size;
+  float a = ceilf(((lo + 1.0f) * s - 1.0f) * 0.5f);
+  float b = floorf(((hi + 1.0f) * s - 1.0f) * 0.5f);
+  a = fminf(fmaxf(a, 0.0f), s);
+  b = fminf(fmaxf(b, -1.0f), s - 1.0f);
+  i0 = (int)a;
+  i1 = (int)b;
 }
 
-__device__ __forceinline__ void span_minmax(float m, float d0, float d1, float* lo, float* hi, float* mag) {
-  const float a = m * d0, b = m * d1;
-  *lo = fminf(a, b);
-  *hi = fmaxf(a, b);
-  *mag = fmaxf(fabsf(a), fabsf(b));
-}
-
-__device__ __forceinline__ bool tile_hit(float4 q0, float4 q1, int tx, int ty, u32 width, u32 height) {
-  const int px0 = tx * (int)kTile, py0 = ty * (int)kTile;
-  const int px1 = min(px0 + (int)kTile - 1, (int)width - 1), py1 = min(py0 + (int)kTile - 1, (int)height - 1);
-  const float dx0 = pixel_ndc(px0, width) - q0.x, dx1 = pixel_ndc(px1, width) - q0.x;
-  const float dy0 = pixel_ndc(py0, height) - q0.y, dy1 = pixel_ndc(py1, height) - q0.y;
-  float l0, h0, g0, l1, h1, g1;
-  span_minmax(q0.z, dx0, dx1, &l0, &h0, &g0);  // m00 * dx
-  span_minmax(q0.w, dy0, dy1, &l1, &h1, &g1);  // m01 * dy
-  const float eu = 1e-3f + 1e-5f * (g0 + g1);
-  if (l0 + l1 > 3.0f + eu || h0 + h1 < -3.0f - eu) return false;
-  span_minmax(q1.x, dx0, dx1, &l0, &h0, &g0);  // m10 * dx
-  span_minmax(q1.y, dy0, dy1, &l1, &h1, &g1);  // m11 * dy
-  const float ev = 1e-3f + 1e-5f * (g0 + g1);
-  return !(l0 + l1 > 3.0f + ev || h0 + h1 < -3.0f - ev);
-}
-
-__global__ __launch_bounds__(kBinThreads) void k_bin(const BinArgs a) {
-  __shared__ u32 s_scan[32];
-  __shared__ u32 s_base;
-  __shared__ u32 s_part;
-  const u32 tid = threadIdx.x;
-  const u32 v = min(*a.visible_count, a.n);
-  const u32 nparts = (v + kBinTile - 1) / kBinTile;
-  for (;;) {
-    if (tid == 0) s_part = atomicAdd(a.ticket, 1u);
-    __syncthreads();
-    const u32 p = s_part;
-    if (p >= nparts) break;
-    const u32 r0 = p * kBinTile + tid * kBinItems;
-    u32 id[kBinItems], cnt[kBinItems];
-    float4 q0[kBinItems], q1[kBinItems];
-    TileRect rect[kBinItems];
-    u32 sum = 0;
+// Loads the splat's raster record; false when it is not drawn.
+__device__ __forceinline__ bool footprint(const float4* __restrict__ record, u32 id, const TargetGeom& g,
+                                          Footprint& f) {
+  const float4* r = record + 4 * (size_t)id;
+  const float4 q2 = __ldg(r + 2);
+  if (!(q2.w > 0.0f)) return false;
+  const float4 q0 = __ldg(r + 0), q3 = __ldg(r + 3);
+  const float cx = q0.x, cy = q0.y;
+  const float ax = 3.0f * q3.x, ay = 3.0f * q3.y, bx = 3.0f * q3.z, by = 3.0f * q3.w;
+  f.vx[0] = cx - ax - bx, f.vy[0] = cy - ay - by;
+  f.vx[1] = cx + ax - bx, f.vy[1] = cy + ay - by;
+  f.vx[2] = cx + ax + bx, f.vy[2] = cy + ay + by;
+  f.vx[3] = cx - ax + bx, f.vy[3] = cy - ay + by;
 #pragma unroll
-    for (u32 k = 0; k < kBinItems; ++k) {
-      cnt[k] = 0;
-      rect[k] = TileRect{0, -1, 0, -1};
-      id[k] = 0;
-      if (r0 + k < v) {
-        id[k] = a.index[r0 + k];
-        const float4* rec = a.record + 4 * (size_t)id[k];
-        q0[k] = rec[0];
-        q1[k] = rec[1];
-        rect[k] = tile_rect(q0[k], rec[3], a.width, a.height);
-        for (int ty = rect[k].ty0; ty <= rect[k].ty1; ++ty)
-          for (int tx = rect[k].tx0; tx <= rect[k].tx1; ++tx)
-            cnt[k] += tile_hit(q0[k], q1[k], tx, ty, a.width, a.height) ? 1u : 0u;
-      }
-      sum += cnt[k];
-    }
-    u32 ptot;
-    const u32 excl_t = block_exclusive_scan<kBinThreads>(sum, s_scan, &ptot);
-    if (tid == 0) {
-      const u32 excl = lookback(a.status, 1, p, a.epoch, ptot, a.err);
-      s_base = excl;
-      if (p == nparts - 1) {
-        const u32 total = excl + ptot;
-        *a.pair_total = total;
-        *a.pair_count = min(total, a.pair_capacity);
-        if (total > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
-      }
-    }
-    __syncthreads();
-    u32 pos = s_base + excl_t;
-#pragma unroll
-    for (u32 k = 0; k < kBinItems; ++k) {
-      if (!cnt[k]) continue;
-      for (int ty = rect[k].ty0; ty <= rect[k].ty1; ++ty)
-        for (int tx = rect[k].tx0; tx <= rect[k].tx1; ++tx)
-          if (tile_hit(q0[k], q1[k], tx, ty, a.width, a.height)) {
-            if (pos < a.pair_capacity) {
-              a.pair_tile[pos] = (u32)ty * a.tiles_x + (u32)tx;
-              a.pair_splat[pos] = id[k];
-            }
-            ++pos;
-          }
-    }
-    __syncthreads();
+  for (int k = 0; k < 4; ++k) {
+    const int n = (k + 1) & 3;
+    f.dxdy[k] = (f.vx[n] - f.vx[k]) / (f.vy[n] - f.vy[k]);  // +-inf/NaN for horizontal edges: never used
+  }
+  const float h = fabsf(ay) + fabsf(by) + 2.0f * kMarginPx * g.inv_h;
+  int y0, y1;
+  pixel_range(cy - h, cy + h, g.height, y0, y1);
+  f.ty0 = y0 / (int)kTile;
+  f.ty1 = y1 < y0 ? f.ty0 - 1 : y1 / (int)kTile;
+  return true;
+}
+
+__device__ __forceinline__ void clip_edge(const Footprint& f, int k, float y, float& xmin, float& xmax) {
+  const int n = (k + 1) & 3;
+  if ((f.vy[k] - y) * (f.vy[n] - y) < 0.0f) {
+    const float x = f.vx[k] + (y - f.vy[k]) * f.dxdy[k];
+    xmin = fminf(xmin, x);
+    xmax = fmaxf(xmax, x);
   }
 }
 
-cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream) {
-  if (a.n == 0) return cudaSuccess;
-  const u32 parts = (a.n + kBinTile - 1) / kBinTile;
-  const int sms = a.num_sms > 0 ? a.num_sms : 1;
-  const u32 grid = min(parts, (u32)sms * 8u);
-  k_bin<<<grid, kBinThreads, 0, stream>>>(a);
-  return cudaGetLastError();
+// Tile columns [tx0, tx1] of tile row ty reached by the quad (empty when tx0 > tx1).
+__device__ __forceinline__ void footprint_cols(const Footprint& f, const TargetGeom& g, int ty, int& tx0, int& tx1) {
+  const int r0 = ty * (int)kTile, r1 = min(r0 + (int)kTile - 1, (int)g.height - 1);
+  const float m = 2.0f * kMarginPx * g.inv_h;
+  const float ya = (float)(2 * r0 + 1) * g.inv_h - 1.0f - m;
+  const float yb = (float)(2 * r1 + 1) * g.inv_h - 1.0f + m;
+  float xmin = 3.0e38f, xmax = -3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (f.vy[k] >= ya && f.vy[k] <= yb) {
+      xmin = fminf(xmin, f.vx[k]);
+      xmax = fmaxf(xmax, f.vx[k]);
+    }
+    clip_edge(f, k, ya, xmin, xmax);
+    clip_edge(f, k, yb, xmin, xmax);
+  }
+  tx0 = 0;
+  tx1 = -1;
+  if (!(xmin <= xmax)) return;
+  const float mx = 2.0f * kMarginPx * g.inv_w;
+  int x0, x1;
+  pixel_range(xmin - mx, xmax + mx, g.width, x0, x1);
+  if (x0 > x1) return;
+  tx0 = x0 / (int)kTile;
+  tx1 = x1 / (int)kTile;
 }
 
+__device__ __forceinline__ u32 footprint_pairs(const Footprint& f, const TargetGeom& g) {
+  u32 n = 0;
+  for (int ty = f.ty0; ty <= f.ty1; ++ty) {
+    int tx0, tx1;
+    footprint_cols(f, g, ty, tx0, tx1);
+    n += (u32)max(0, tx1 - tx0 + 1);
+  }
+  return n;
+}
+
+__device__ __forceinline__ u32 visible(const BinArgs& a) { return min(*a.visible_count, a.n); }
+
+// 1. pairs per sorted splat
+__global__ __launch_bounds__(kCountThreads) void k_bin_count(const BinArgs a) {
+  const u32 v = visible(a);
+  const TargetGeom g = target_geom(a);
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 r = blockIdx.x * blockDim.x + threadIdx.x; r < v; r += stride) {
+    Footprint f;
+    a.count[r] = footprint(a.record, __ldg(a.index + r), g, f) ? footprint_pairs(f, g) : 0u;
+  }
+}
+
+// 2a. per-block sums of count[]
+__global__ __launch_bounds__(kScanThreads) void k_bin_reduce(const BinArgs a) {
+  __shared__ u32 s_scan[32];
+  const u32 v = visible(a);
+  const u32 base = blockIdx.x * kScanTile;
+  if (base >= v) return;
+  u32 s = 0;
+#pragma unroll
+  for (u32 i = 0; i < kScanItems; ++i) {
+    const u32 r = base + i * kScanThreads + threadIdx.x;
+    s += r < v ? a.count[r] : 0u;
+  }
+  u32 total;
+  block_exclusive_scan<kScanThreads>(s, s_scan, &total);
+  if (threadIdx.x == 0) a.block_sum[blockIdx.x] = total;
+}
+
+// 2b. exclusive scan of the block sums (one CTA), the pair total and the capacity check
+__global__ __launch_bounds__(1024) void k_bin_scan_blocks(const BinArgs a) {
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_carry;
+  const u32 nblocks = (visible(a) + kScanTile - 1) / kScanTile;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (u32 b0 = 0; b0 < nblocks; b0 += 1024) {
+    const u32 b = b0 + threadIdx.x;
+    const u32 x = b < nblocks ? a.block_sum[b] : 0u;
+    u32 sum;
+    const u32 excl = block_exclusive_scan<1024>(x, s_scan, &sum);
+    if (b < nblocks) a.block_sum[b] = s_carry + excl;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += sum;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const u32 P = s_carry;
+    *a.pair_total = P;
+    *a.pair_count = min(P, a.pair_capacity);
+    if (P > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
+  }
+}
+
+// 2c. count[] -> exclusive prefix (first pair of each splat), in place
+__global__ __launch_bounds__(kScanThreads) void k_bin_scan(const BinArgs a) {
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_vals[kScanTile];
+  const u32 v = visible(a);
+  const u32 base = blockIdx.x * kScanTile;
+  if (base >= v) return;
+  // blocked arrangement: thread t owns elements [t*items, (t+1)*items) of the block
+  for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+    const u32 r = base + i;
+    s_vals[i] = r < v ? a.count[r] : 0u;
+  }
+  __syncthreads();
+  u32 x[kScanItems], s = 0;
+#pragma unroll
+  for (u32 i = 0; i < kScanItems; ++i) {
+    x[i] = s_vals[threadIdx.x * kScanItems + i];
+    s += x[i];
+  }
+  u32 total;
+  u32 run = a.block_sum[blockIdx.x] + block_exclusive_scan<kScanThreads>(s, s_scan, &total);
+#pragma unroll
+  for (u32 i = 0; i < kScanItems; ++i) {
+    s_vals[threadIdx.x * kScanItems + i] = run;
+    run += x[i];
+  }
+  __syncthreads();
+  for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+    const u32 r = base + i;
+    if (r < v) a.count[r] = s_vals[i];
+  }
+}
+
+// 3. emission: warp w expands the pairs of 32 consecutive sorted splats, in order, and stores them
+//    coalesced into their contiguous output range.
+__global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
+  __shared__ u32 s_tile[kEmitWarps][kEmitBuf];
+  __shared__ u32 s_lane[kEmitWarps][kEmitBuf];
+  const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  u32* btile = s_tile[warp];
+  u32* blane = s_lane[warp];
+  const u32 v = visible(a);
+  const u32 P = *a.pair_total;
+  const TargetGeom g = target_geom(a);
+  const u32 gwarps = gridDim.x * kEmitWarps;
+  for (u32 r0 = (blockIdx.x * kEmitWarps + warp) * 32; r0 < v; r0 += gwarps * 32) {
+    const u32 r = r0 + lane;
+    Footprint f;
+    f.ty0 = 0;
+    f.ty1 = -1;
+    u32 id = 0, first = 0;
+    if (r < v) {
+      id = __ldg(a.index + r);
+      first = a.count[r];  // exclusive prefix after the scan
+      if (!footprint(a.record, id, g, f)) f.ty1 = f.ty0 - 1;
+    }
+    const u32 n = footprint_pairs(f, g);
+    const u32 wfirst = __shfl_sync(0xffffffffu, first, 0);
+    const u32 last_end = __shfl_sync(0xffffffffu, r < v ? first + n : 0u, min(31u, v - 1 - r0));
+    if (r < v) {
+      const u32 expect_end = r + 1 < v ? a.count[r + 1] : P;
+      if (first + n != expect_end) atomicOr(a.err, ERR_INTERNAL);
+    }
+    const u32 total = last_end - wfirst;
+    // resumable cursor over this lane's pairs (row-major)
+    u32 k = first - wfirst;
+    int cty = f.ty0, ctx = 0, ctx1 = -1;
+    if (n) {
+      for (; cty <= f.ty1; ++cty) {
+        footprint_cols(f, g, cty, ctx, ctx1);
+        if (ctx <= ctx1) break;
+      }
+    }
+    const u32 kend = k + n;
+    for (u32 w0 = 0; w0 < total; w0 += kEmitBuf) {
+      while (k < kend && k < w0 + kEmitBuf) {  // k >= w0 on entry to every window
+        btile[k - w0] = (u32)(cty * (int)a.tiles_x + ctx);
+        blane[k - w0] = lane;
+        ++k;
+        if (++ctx > ctx1) {
+          for (++cty; cty <= f.ty1; ++cty) {
+            footprint_cols(f, g, cty, ctx, ctx1);
+            if (ctx <= ctx1) break;
+          }
+        }
+      }
+      __syncwarp();
+      const u32 m = min((u32)kEmitBuf, total - w0);
+      for (u32 j0 = 0; j0 < m; j0 += 32) {
+        const u32 j = j0 + lane;
+        const bool has = j < m;
+        const u32 oid = __shfl_sync(0xffffffffu, id, has ? blane[j] : 0u);
+        const u32 pos = wfirst + w0 + j;
+        if (has && pos < a.pair_capacity) {
+          a.pair_tile[pos] = btile[j];
+          a.pair_splat[pos] = oid;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// 4. tile ranges from the tile-sorted pair keys
 __global__ void k_tile_ranges(const u32* __restrict__ tile, const u32* __restrict__ pair_count, u32 capacity,
                               uint2* __restrict__ range) {
   const u32 P = min(*pair_count, capacity);
@@ -152,10 +295,32 @@ __global__ void k_tile_ranges(const u32* __restrict__ tile, const u32* __restric
   }
 }
 
+size_t bin_block_sums(u32 max_splats) { return (max(max_splats, 1u) + kScanTile - 1) / kScanTile; }
+
+cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_count, cudaEvent_t after_scan,
+                       int num_sms) {
+  if (a.n == 0) {
+    if (after_count) cudaEventRecord(after_count, stream);
+    if (after_scan) cudaEventRecord(after_scan, stream);
+    return cudaSuccess;
+  }
+  const u32 sms = (u32)max(num_sms, 1);
+  const u32 count_grid = min((a.n + kCountThreads - 1) / kCountThreads, sms * 16u);
+  k_bin_count<<<count_grid, kCountThreads, 0, stream>>>(a);
+  if (after_count) cudaEventRecord(after_count, stream);
+  const u32 blocks = (u32)bin_block_sums(a.n);
+  k_bin_reduce<<<blocks, kScanThreads, 0, stream>>>(a);
+  k_bin_scan_blocks<<<1, 1024, 0, stream>>>(a);
+  k_bin_scan<<<blocks, kScanThreads, 0, stream>>>(a);
+  if (after_scan) cudaEventRecord(after_scan, stream);
+  const u32 emit_grid = min((a.n + kEmitThreads - 1) / kEmitThreads, sms * 8u);
+  k_bin_emit<<<emit_grid, kEmitThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tile_ranges(const u32* pair_tile, const u32* pair_count, u32 capacity, u32* tile_range,
                                int num_sms, cudaStream_t stream) {
-  const int sms = num_sms > 0 ? num_sms : 1;
-  const u32 grid = max(1u, min((capacity + 255) / 256, (u32)sms * 8u));
+  const u32 grid = max(1u, min((capacity + 255) / 256, (u32)max(num_sms, 1) * 8u));
   k_tile_ranges<<<grid, 256, 0, stream>>>(pair_tile, pair_count, capacity, reinterpret_cast<uint2*>(tile_range));
   return cudaGetLastError();
 }

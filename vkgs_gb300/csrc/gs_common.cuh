@@ -13,6 +13,7 @@ typedef uint64_t u64;
 enum : u32 {
   ERR_CAPACITY = 1u,  // more (splat, tile) pairs than the context holds, or a sort count beyond max_count
   ERR_TIMEOUT = 2u,   // a bounded look-back wait gave up
+  ERR_INTERNAL = 4u,  // a self-check failed (e.g. emitted tile pairs disagree with the counted ones)
 };
 
 // Upper bound on polls of one look-back status word.  A predecessor partition publishes its

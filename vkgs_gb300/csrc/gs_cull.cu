@@ -154,9 +154,8 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
   float4* rec = a.record + 4 * (size_t)id;
   rec[0] = make_float4(nx, ny, m00, m01);
   rec[1] = make_float4(m10, m11, nz, o);
-  rec[2] = make_float4(fminf(color[0], 1.0f), fminf(color[1], 1.0f), fminf(color[2], 1.0f), 0.0f);
-  rec[3] = drawn ? make_float4(3.0f * (fabsf(rs0) + fabsf(rs2)), 3.0f * (fabsf(rs1) + fabsf(rs3)), 0.0f, 0.0f)
-                 : make_float4(-1.0f, -1.0f, 0.0f, 0.0f);
+  rec[2] = make_float4(fminf(color[0], 1.0f), fminf(color[1], 1.0f), fminf(color[2], 1.0f), drawn ? 1.0f : 0.0f);
+  rec[3] = make_float4(rs0, rs1, rs2, rs3);
   if (a.inst_by_id) {
     float4* inst = reinterpret_cast<float4*>(a.inst_by_id + 12 * (size_t)id);
     inst[0] = make_float4(nx, ny, nz, 0.0f);

@@ -61,10 +61,8 @@ cudaError_t launch_instances(const u32* index, const u32* visible_count, const f
                              float* instances, u32* draw_indirect, cudaStream_t stream);
 
 // ---- tile binning (gs_bin.cu) ----
-constexpr u32 kTile = 16;  // tile edge in pixels
-constexpr u32 kBinThreads = 256;
-constexpr u32 kBinItems = 4;
-constexpr u32 kBinTile = kBinThreads * kBinItems;
+constexpr u32 kTile = 16;            // tile edge in pixels
+constexpr u32 kMaxTiles = 1u << 24;  // tile ids must stay below 2^24 (radix passes on the tile id)
 
 struct BinArgs {
   const u32* index;          // sorted splat ids
@@ -72,24 +70,27 @@ struct BinArgs {
   const float4* record;
   u32 n;                     // launch bound for V
   u32 width, height, tiles_x, tiles_y;
-  u32* pair_tile;            // out: tile id per pair
+  u32* count;                // [n] pairs per sorted splat, then its first pair (exclusive prefix)
+  u32* block_sum;            // [bin_block_sums(n)]
+  u32* pair_tile;            // out: tile id per pair, pairs in sorted-splat order
   u32* pair_splat;           // out: splat id per pair
   u32 pair_capacity;
   u32* pair_count;           // out: min(total, capacity)
   u32* pair_total;           // out: pairs needed
-  u64* status;
-  u32* ticket;
-  u32 epoch;
   u32* err;
-  int num_sms;
 };
-cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream);
+
+size_t bin_block_sums(u32 max_splats);
+// Records after_count / after_scan (when non-null) between the count, scan and emit steps.
+cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_count, cudaEvent_t after_scan,
+                       int num_sms);
 cudaError_t launch_tile_ranges(const u32* pair_tile, const u32* pair_count, u32 capacity, u32* tile_range /*2*T*/,
                                int num_sms, cudaStream_t stream);
 
 // ---- raster (gs_raster.cu) ----
 struct RasterArgs {
-  const u32* tile_range;     // [T][2] = (begin, end)
+  const u32* tile_range;     // [T][2] = (begin, end) into pair_splat
+  u32 pair_capacity;
   const u32* pair_splat;
   const float4* record;
   u32 width, height, tiles_x, tiles_y;
@@ -97,7 +98,8 @@ struct RasterArgs {
   uchar4* out_bgra;          // may be null
   const float* depth;        // may be null
   float t_floor;             // blending stops once every pixel of a tile is below this transmittance
-  unsigned long long* fragments;  // non-null: count fragments (disables the early stop)
+  unsigned long long* fragments;  // non-null: [0] covered fragments, [1] those met while T >= t_floor
+                                  // (disables the early stop)
 };
 cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
 

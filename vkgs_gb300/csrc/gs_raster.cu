@@ -32,10 +32,11 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   const float fx = __fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f;
   const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
   const float dpix = (DEPTH && inside) ? a.depth[(size_t)py * a.width + px] : 1.0f;
-  const uint2 range = reinterpret_cast<const uint2*>(a.tile_range)[tile];
+  const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range)[tile];
+  const uint2 range = make_uint2(min(tr.x, a.pair_capacity), min(tr.y, a.pair_capacity));
 
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, ca = 0.0f;
-  u32 frags = 0;
+  u32 frags = 0, needed = 0;
   const float kExp = -0.5f * 1.4426950408889634f;  // -log2(e)/2
   bool done = !inside;
   for (u32 hi = range.y; hi > range.x;) {
@@ -57,7 +58,10 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
         const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
         bool cov = (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
         if (DEPTH) cov &= q1.z < dpix;
-        if (COUNT) frags += (cov && inside) ? 1u : 0u;
+        if (COUNT) {
+          frags += (cov && inside) ? 1u : 0u;
+          needed += (cov && inside && T >= a.t_floor) ? 1u : 0u;
+        }
         const float g = exp2f(kExp * (u * u + v * v));
         const float al = cov ? q1.w * g : 0.0f;
         const float w = al * T;
@@ -76,8 +80,12 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   }
   if (COUNT) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      frags += __shfl_xor_sync(0xffffffffu, frags, o);
+      needed += __shfl_xor_sync(0xffffffffu, needed, o);
+    }
     if ((tid & 31) == 0 && frags) atomicAdd(a.fragments, (unsigned long long)frags);
+    if ((tid & 31) == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
   }
   if (!inside) return;
   const size_t pix = (size_t)py * a.width + px;
