@@ -78,6 +78,22 @@ gs_status gs_sorter_sort_key_value_indirect(gs_sorter* sorter, gs_stream stream,
 /* Reads back and clears the sorter's device error word (synchronises the stream). */
 gs_status gs_sorter_check(gs_sorter* sorter, gs_stream stream);
 
+/* No counterpart in the reference.  The same sort for callers that may not allocate device memory
+ * (an engine callback that owns the whole memory budget, code running while other streams are in
+ * flight -- cudaMalloc/cudaFree can synchronise the device -- or code recorded during stream
+ * capture): no sorter handle, no storage argument, and no cudaMalloc/cudaFree on any path.  Its
+ * scratch is one fixed device array inside this library (about 8.4 MB, held by every GPU that
+ * loads the library until the process exits), so max_count may not exceed
+ * GS_SORT_NOALLOC_MAX_COUNT (GS_ERROR_CAPACITY otherwise).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array: calls that may overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller.  device_error (optional device
+ * word) receives the error bits: 1 = *count exceeded max_count and was clamped, 2 = a bounded device
+ * wait gave up. */
+#define GS_SORT_NOALLOC_MAX_COUNT (1u << 20)
+gs_status gs_sort_key_value_noalloc(gs_stream stream, uint32_t max_count, const uint32_t* count, uint32_t* keys,
+                                    uint32_t* values, uint32_t* device_error);
+
 /* ------------------------------------------------------------------------ */
 /* Splat buffers, camera, target                                             */
 /* ------------------------------------------------------------------------ */

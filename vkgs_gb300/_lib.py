@@ -20,6 +20,7 @@ GS_ERROR_DEVICE_TIMEOUT = 4
 GS_ERROR_OUT_OF_MEMORY = 5
 GS_ERROR_INTERNAL = 6
 GS_NUM_STAGES = 6
+GS_SORT_NOALLOC_MAX_COUNT = 1 << 20  # include/vkgs_gb300.h
 STAGES = ("cull_project", "depth_sort", "bin", "tile_sort", "tile_ranges", "raster")
 
 
@@ -66,6 +67,7 @@ SIGNATURES = [
     ("gs_sorter_sort_key_value_indirect", c_int,
      [c_void_p, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t]),
     ("gs_sorter_check", c_int, [c_void_p, c_void_p]),
+    ("gs_sort_key_value_noalloc", c_int, [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("gs_context_create", c_int, [POINTER(c_void_p), POINTER(GsContextOptions)]),
     ("gs_context_destroy", None, [c_void_p]),
     ("gs_context_reserve", c_int, [c_void_p, POINTER(GsContextOptions)]),

@@ -32,6 +32,7 @@ UNITS = {
     # the count and emit kernels evaluate the same tile-footprint arithmetic and must agree exactly
     "gs_bin.cu": ["--fmad=false"],
     "gs_raster.cu": ["-ftz=true"],
+    "gs_noalloc.cu": [],
 }
 HEADERS = ["gs_common.cuh", "gs_internal.h"]
 
