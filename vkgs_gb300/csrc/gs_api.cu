@@ -7,7 +7,7 @@
 //   vrdxCmdSortKeyValueIndirect                 onesweep radix sort of (key, index), count on device
 //   fill(inverse, -1) + inverse_index.comp      (not needed: records are keyed by splat id)
 //   projection.comp                             (fused into the cull pass)
-//   vkCmdDrawIndexedIndirect + blend            tile binning -> stable tile sort -> tile raster
+//   vkCmdDrawIndexedIndirect + blend            ordered tile binning -> stable tile-id sort -> tile raster
 // Nothing here synchronises the host or allocates after gs_context_create/gs_context_reserve.
 #include <cuda_runtime.h>
 

@@ -5,8 +5,10 @@
 // each 16x16 tile receives the list of splats whose 3-sigma quad can cover one of its pixel centres:
 //   1. count : per sorted splat, the number of tiles its quad reaches -> count[r]
 //   2. scan  : exclusive scan of count[] -> first[r] and the pair total P (reduce-then-scan, no waits)
-//   3. emit  : each warp expands the pairs of 32 consecutive sorted splats in order into shared memory
-//              and stores them coalesced at [first[r0], ...): pairs leave in ascending sorted position
+//   3. emit  : each warp lists the row spans of 32 consecutive sorted splats in shared memory and its
+//              lanes take consecutive pairs (span found by binary search), storing them coalesced at
+//              [first[r0], ...): pairs leave in ascending sorted position, and a splat covering
+//              thousands of tiles is spread over the whole warp
 //   4. a stable radix sort on the tile id alone (gs_sort.cu) then groups them by tile without
 //      disturbing that order, and tile ranges are read off the sorted tile ids.
 // The tile test is exact up to a small margin: the quad (corners c +- a +- b) is clipped to each tile
@@ -21,7 +23,6 @@ namespace gs {
 constexpr u32 kCountThreads = 256;
 constexpr u32 kEmitThreads = 256;
 constexpr u32 kEmitWarps = kEmitThreads / 32;
-constexpr u32 kEmitBuf = 512;       // expanded pairs per warp and window
 constexpr u32 kScanThreads = 256;
 constexpr u32 kScanItems = 16;
 constexpr u32 kScanTile = kScanThreads * kScanItems;  // counts per scan block
@@ -213,14 +214,97 @@ __global__ __launch_bounds__(kScanThreads) void k_bin_scan(const BinArgs a) {
   }
 }
 
-// 3. emission: warp w expands the pairs of 32 consecutive sorted splats, in order, and stores them
-//    coalesced into their contiguous output range.
+constexpr u32 kSpanBuf = 128;  // row spans per warp and window
+
+// Walks the (splat, tile) pairs of 32 consecutive sorted splats (lane = splat; ok = drawn) in sorted
+// order -- splat by splat, row-major inside a splat -- 32 pairs per step, and calls
+// fn(has, tile, owner_lane, j) on every lane of the warp for each step (j = the pair's index among the
+// 32 splats' pairs); returns the number of pairs.  The splats' row spans are listed
+// in shared memory (span = one tile row of one splat) with an exclusive prefix of their widths, so a
+// lane finds the span of pair j by binary search and no lane expands a footprint serially: a splat
+// that covers thousands of tiles costs the whole warp as much as that many small splats.
+// s_span: 2 * (kSpanBuf + 1) words of this warp's shared memory.  Whole warp.
+template <class F>
+__device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const TargetGeom& g, u32* s_span, F&& fn) {
+  u32* s_tile = s_span;                // tile id of the span's first column << 5 | owner lane
+  u32* s_pfx = s_span + kSpanBuf + 1;  // exclusive prefix of the span widths, [m] = total
+  const u32 lane = threadIdx.x & 31u;
+  const u32 nrows = ok ? (u32)max(0, f.ty1 - f.ty0 + 1) : 0u;
+  u32 incl = nrows;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (u32)o) incl += y;
+  }
+  const u32 rfirst = incl - nrows;
+  const u32 total_rows = __shfl_sync(0xffffffffu, incl, 31);
+  u32 done = 0;  // pairs of earlier windows
+  for (u32 rw0 = 0; rw0 < total_rows; rw0 += kSpanBuf) {
+    const u32 i0 = max(rw0, rfirst), i1 = min(rfirst + nrows, rw0 + kSpanBuf);
+    for (u32 i = i0; i < i1; ++i) {
+      const int ty = f.ty0 + (int)(i - rfirst);
+      int tx0, tx1;
+      footprint_cols(f, g, ty, tx0, tx1);
+      s_tile[i - rw0] = ((u32)(ty * (int)g.tiles_x + max(tx0, 0)) << 5) | lane;
+      s_pfx[i - rw0] = (u32)max(0, tx1 - tx0 + 1);  // width for now
+    }
+    __syncwarp();
+    const u32 m = min(kSpanBuf, total_rows - rw0);
+    // exclusive scan of the m widths in place: each lane owns kSpanBuf/32 consecutive entries
+    constexpr u32 kPer = kSpanBuf / 32;
+    u32 w[kPer], s = 0;
+#pragma unroll
+    for (u32 q = 0; q < kPer; ++q) {
+      const u32 e = lane * kPer + q;
+      w[q] = e < m ? s_pfx[e] : 0u;
+      s += w[q];
+    }
+    u32 sincl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 y = __shfl_up_sync(0xffffffffu, sincl, o);
+      if (lane >= (u32)o) sincl += y;
+    }
+    const u32 pairs = __shfl_sync(0xffffffffu, sincl, 31);
+    u32 run = sincl - s;
+    __syncwarp();
+#pragma unroll
+    for (u32 q = 0; q < kPer; ++q) {
+      const u32 e = lane * kPer + q;
+      if (e < m) s_pfx[e] = run;
+      run += w[q];
+    }
+    if (lane == 0) s_pfx[m] = pairs;
+    __syncwarp();
+    for (u32 j0 = 0; j0 < pairs; j0 += 32) {
+      const u32 j = j0 + lane;
+      const bool has = j < pairs;
+      u32 tile = 0, owner = 0;
+      if (has) {
+        u32 lo = 0, hi = m;  // last span with s_pfx[span] <= j
+        while (hi - lo > 1) {
+          const u32 mid = (lo + hi) >> 1;
+          if (s_pfx[mid] <= j) lo = mid;
+          else hi = mid;
+        }
+        const u32 e = s_tile[lo];
+        tile = (e >> 5) + (j - s_pfx[lo]);
+        owner = e & 31u;
+      }
+      fn(has, tile, owner, done + j);
+    }
+    done += pairs;
+    __syncwarp();
+  }
+  return done;
+}
+
+// 3. emission: warp w walks 32 consecutive sorted splats' pairs -- splat by splat, row-major inside a
+//    splat -- with the span list of for_each_pair, and stores them coalesced into their contiguous
+//    output range [first[r0], ...): pairs leave in ascending sorted position.
 __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
-  __shared__ u32 s_tile[kEmitWarps][kEmitBuf];
-  __shared__ u32 s_lane[kEmitWarps][kEmitBuf];
+  __shared__ u32 s_spans[kEmitWarps][2 * (kSpanBuf + 1)];
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  u32* btile = s_tile[warp];
-  u32* blane = s_lane[warp];
   const u32 v = visible(a);
   const u32 P = *a.pair_total;
   const TargetGeom g = target_geom(a);
@@ -228,58 +312,24 @@ __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
   for (u32 r0 = (blockIdx.x * kEmitWarps + warp) * 32; r0 < v; r0 += gwarps * 32) {
     const u32 r = r0 + lane;
     Footprint f;
-    f.ty0 = 0;
-    f.ty1 = -1;
-    u32 id = 0, first = 0;
+    bool ok = false;
+    u32 id = 0;
     if (r < v) {
       id = __ldg(a.index + r);
-      first = a.count[r];  // exclusive prefix after the scan
-      if (!footprint(a.record, id, g, f)) f.ty1 = f.ty0 - 1;
+      ok = footprint(a.record, id, g, f);
     }
-    const u32 n = footprint_pairs(f, g);
-    const u32 wfirst = __shfl_sync(0xffffffffu, first, 0);
-    const u32 last_end = __shfl_sync(0xffffffffu, r < v ? first + n : 0u, min(31u, v - 1 - r0));
-    if (r < v) {
-      const u32 expect_end = r + 1 < v ? a.count[r + 1] : P;
-      if (first + n != expect_end) atomicOr(a.err, ERR_INTERNAL);
-    }
-    const u32 total = last_end - wfirst;
-    // resumable cursor over this lane's pairs (row-major)
-    u32 k = first - wfirst;
-    int cty = f.ty0, ctx = 0, ctx1 = -1;
-    if (n) {
-      for (; cty <= f.ty1; ++cty) {
-        footprint_cols(f, g, cty, ctx, ctx1);
-        if (ctx <= ctx1) break;
+    const u32 gfirst = a.count[r0];  // exclusive prefix after the scan
+    const u32 rl = min(r0 + 32u, v);
+    const u32 gend = rl < v ? a.count[rl] : P;
+    const u32 total = for_each_pair(f, ok, g, s_spans[warp], [&](bool has, u32 tile, u32 owner, u32 j) {
+      const u32 oid = __shfl_sync(0xffffffffu, id, owner);
+      const u32 pos = gfirst + j;
+      if (has && pos < a.pair_capacity) {
+        a.pair_tile[pos] = tile;
+        a.pair_splat[pos] = oid;
       }
-    }
-    const u32 kend = k + n;
-    for (u32 w0 = 0; w0 < total; w0 += kEmitBuf) {
-      while (k < kend && k < w0 + kEmitBuf) {  // k >= w0 on entry to every window
-        btile[k - w0] = (u32)(cty * (int)a.tiles_x + ctx);
-        blane[k - w0] = lane;
-        ++k;
-        if (++ctx > ctx1) {
-          for (++cty; cty <= f.ty1; ++cty) {
-            footprint_cols(f, g, cty, ctx, ctx1);
-            if (ctx <= ctx1) break;
-          }
-        }
-      }
-      __syncwarp();
-      const u32 m = min((u32)kEmitBuf, total - w0);
-      for (u32 j0 = 0; j0 < m; j0 += 32) {
-        const u32 j = j0 + lane;
-        const bool has = j < m;
-        const u32 oid = __shfl_sync(0xffffffffu, id, has ? blane[j] : 0u);
-        const u32 pos = wfirst + w0 + j;
-        if (has && pos < a.pair_capacity) {
-          a.pair_tile[pos] = btile[j];
-          a.pair_splat[pos] = oid;
-        }
-      }
-      __syncwarp();
-    }
+    });
+    if (lane == 0 && gfirst + total != gend) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
   }
 }
 

@@ -37,6 +37,19 @@ __device__ __forceinline__ u32 lanemask_lt() {
   return m;
 }
 
+// Lanes of the warp whose 8-bit digit equals this lane's, among the lanes in `active` (8 ballots;
+// faster than __match_any_sync on this architecture).  Must be called by the whole warp.
+__device__ __forceinline__ u32 match_digit8(u32 d, bool active) {
+  u32 peers = __ballot_sync(0xffffffffu, active);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const u32 bb = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  return peers;
+}
+
 // Decoupled look-back status word: [63:32] epoch, [31:30] flag, [29:0] value.  A word whose epoch
 // differs from the caller's is "not yet published" for this pass, so the status array never needs
 // clearing between passes or frames.

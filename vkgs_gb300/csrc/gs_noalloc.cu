@@ -29,7 +29,7 @@ constexpr size_t round_words(size_t w) { return (w + kAlignWords - 1) / kAlignWo
 // Layout of the scratch, in 32-bit words: control block | error word | status (u64) | keys_alt | values_alt
 constexpr size_t kControlWords = round_words(kRadixControlBytes / sizeof(u32));
 constexpr size_t kErrorWords = kAlignWords;
-constexpr size_t kStatusWords = round_words(2 * ((size_t)(kMaxCount + 4095) / 4096) * 256);
+constexpr size_t kStatusWords = round_words(2 * ((size_t)(kMaxCount + kRadixTile - 1) / kRadixTile) * 256);
 constexpr size_t kAltWords = round_words(kMaxCount);
 constexpr size_t kScratchWords = kControlWords + kErrorWords + kStatusWords + 2 * kAltWords;
 

@@ -4,7 +4,7 @@
 // (vrdxCmdSortKeyValueIndirect, src/vkgs/engine/engine.cc:1218-1219): ascending keys, values moved
 // alongside, element count read from device memory.  Design:
 //   * one histogram kernel reads the keys once and counts every 8-bit digit of every pass;
-//   * one "onesweep" kernel per pass: persistent CTAs take 4096-key partitions in ticket order,
+//   * one "onesweep" kernel per pass: CTAs take kRadixTile-key partitions in ticket order,
 //     rank each key inside its warp with 8 ballots (stable: warp-striped loads, items in order),
 //     publish per-digit partition counts through a decoupled look-back (bounded waits, epoch-tagged
 //     status words so nothing is cleared between passes), then stage the partition in shared memory
@@ -16,8 +16,9 @@ namespace gs {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = 16;
+constexpr int RS_ITEMS = kRadixItems;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // keys per partition
+static_assert(RS_TILE == (int)kRadixTile, "partition size");
 constexpr int RS_RADIX = 256;
 constexpr int RS_MAX_PASSES = 4;
 
@@ -46,14 +47,14 @@ __global__ __launch_bounds__(256) void k_radix_histogram(const u32* __restrict__
 }
 
 template <bool HAS_VALUES>
-__global__ __launch_bounds__(RS_THREADS, 2) void k_radix_onesweep(
+__global__ __launch_bounds__(RS_THREADS, 3) void k_radix_onesweep(
     const u32* __restrict__ keys_in, u32* __restrict__ keys_out, const u32* __restrict__ vals_in,
     u32* __restrict__ vals_out, const u32* __restrict__ count_ptr, u32 max_count, const u32* __restrict__ hist,
     u64* __restrict__ status, u32* __restrict__ ticket, u32 epoch, u32 shift, u32* __restrict__ err) {
-  __shared__ u32 s_stage[RS_TILE];
+  __shared__ uint2 s_stage[RS_TILE];   // (key, value) in digit order
   __shared__ u32 s_whist[RS_WARPS][RS_RADIX];
   __shared__ u32 s_goff[RS_RADIX];    // exclusive scan of the global digit histogram
-  __shared__ u32 s_base[RS_RADIX];    // output position of this partition's first key of each digit
+  __shared__ u32 s_delta[RS_RADIX];   // output position minus staged position, per digit
   __shared__ u32 s_lstart[RS_RADIX];  // start of each digit inside the staged partition
   __shared__ u32 s_scan[32];
   __shared__ u32 s_part;
@@ -82,21 +83,18 @@ __global__ __launch_bounds__(RS_THREADS, 2) void k_radix_onesweep(
       if (HAS_VALUES) val[i] = idx < count ? vals_in[idx] : 0u;
     }
     __syncwarp();
+    // Rank every key inside its warp: lanes holding the same digit form a match group, whose lowest
+    // lane reserves the group's slots with one shared-memory atomic (items in order, lanes in order:
+    // the ranking is stable).
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; ++i) {
       const bool valid = wbase + i * 32 + lane < count;
       const u32 d = (key[i] >> shift) & 0xffu;
-      u32 peers = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        const bool bit = (d >> b) & 1u;
-        const u32 bb = __ballot_sync(0xffffffffu, bit);
-        peers &= bit ? bb : ~bb;
-      }
-      const u32 old = s_whist[warp][d];
-      __syncwarp();
-      if (valid && (peers & lt) == 0) s_whist[warp][d] = old + __popc(peers);
-      __syncwarp();
+      const u32 peers = match_digit8(d, valid);
+      const int leader = valid ? __ffs(peers) - 1 : 0;
+      u32 old = 0;
+      if (valid && (int)lane == leader) old = atomicAdd(&s_whist[warp][d], (u32)__popc(peers));
+      old = __shfl_sync(0xffffffffu, old, leader);
       rank[i] = old + __popc(peers & lt);
     }
     __syncthreads();
@@ -110,43 +108,30 @@ __global__ __launch_bounds__(RS_THREADS, 2) void k_radix_onesweep(
       acc += c;
     }
     const u32 excl = lookback(status + tid, RS_RADIX, p, epoch, acc, err);
-    s_base[tid] = s_goff[tid] + excl;
     u32 ptot;
     const u32 lstart = block_exclusive_scan<RS_THREADS>(acc, s_scan, &ptot);
     s_lstart[tid] = lstart;
+    s_delta[tid] = s_goff[tid] + excl - lstart;  // output position = staged position + delta[digit]
     __syncthreads();
 
-    u32 lpos[RS_ITEMS];
+    // Stage (key, value) pairs in digit order, then write them out: consecutive threads hold
+    // consecutive staged pairs, so each digit's run leaves as contiguous stores.
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; ++i) {
       const u32 d = (key[i] >> shift) & 0xffu;
-      lpos[i] = s_lstart[d] + s_whist[warp][d] + rank[i];
-      if (wbase + i * 32 + lane < count) s_stage[lpos[i]] = key[i];
+      const u32 lpos = s_lstart[d] + s_whist[warp][d] + rank[i];
+      if (wbase + i * 32 + lane < count) s_stage[lpos] = make_uint2(key[i], HAS_VALUES ? val[i] : 0u);
     }
     __syncthreads();
     const u32 nvalid = min((u32)RS_TILE, count - base);
-    u32 dig[RS_ITEMS];
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; ++i) {
       const u32 j = tid + i * RS_THREADS;
-      dig[i] = 0;
       if (j < nvalid) {
-        const u32 k = s_stage[j];
-        const u32 d = (k >> shift) & 0xffu;
-        dig[i] = d;
-        keys_out[s_base[d] + j - s_lstart[d]] = k;
-      }
-    }
-    if (HAS_VALUES) {
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < RS_ITEMS; ++i)
-        if (wbase + i * 32 + lane < count) s_stage[lpos[i]] = val[i];
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < RS_ITEMS; ++i) {
-        const u32 j = tid + i * RS_THREADS;
-        if (j < nvalid) vals_out[s_base[dig[i]] + j - s_lstart[dig[i]]] = s_stage[j];
+        const uint2 kv = s_stage[j];
+        const u32 pos = s_delta[(kv.x >> shift) & 0xffu] + j;
+        keys_out[pos] = kv.x;
+        if (HAS_VALUES) vals_out[pos] = kv.y;
       }
     }
     __syncthreads();
@@ -175,7 +160,9 @@ cudaError_t radix_sort(const RadixSortArgs& a, cudaStream_t stream) {
   const u32 max_parts = (a.max_count + RS_TILE - 1) / RS_TILE;
   const u32 hist_grid = (u32)min(max((a.max_count + 256 * 16 - 1) / (256 * 16), 1u), (u32)sms * 4u);
   k_radix_histogram<<<hist_grid, 256, 0, stream>>>(a.keys, a.count, a.max_count, a.begin_bit, passes, hist, a.err);
-  const u32 grid = (u32)max(1u, min(max_parts, (u32)sms * 2u));
+  // One CTA per partition: finished CTAs free their slot for the next partition's loads, so load,
+  // rank and scatter phases of different partitions overlap on every SM.
+  const u32 grid = max(1u, max_parts);
   u32 *ks = a.keys, *vs = a.values, *kd = a.keys_alt, *vd = a.values_alt;
   for (u32 p = 0; p < passes; ++p) {
     if (a.values)
