@@ -10,30 +10,75 @@
 // Here each pixel accumulates the same sum front to back: RGB = sum a_i rgb_i T_i,
 // A = sum a_i^2 T_i + T_end, T_i = prod_{j nearer} (1 - a_j).  The coverage arithmetic uses
 // explicitly rounded operations (no FMA) so that the set of covered (pixel, splat) pairs is exactly
-// the restatement's.  A tile stops once every pixel's transmittance is below t_floor: the splats
-// behind can then change no channel by more than t_floor.
+// the restatement's.  Each warp owns an 8x4 pixel block and walks only the records whose quad can
+// reach that block (a conservative per-batch test), which leaves every pixel's sum unchanged.  A warp
+// stops once its pixels' transmittance is below t_floor, and the tile once all its pixels are: the
+// splats behind can then change no channel by more than t_floor.
 #include "gs_common.cuh"
 #include "gs_internal.h"
 
 namespace gs {
 
 constexpr int kRasterThreads = kTile * kTile;  // one pixel per thread
+constexpr int kWarps = kRasterThreads / 32;
+constexpr int kBlockW = 8, kBlockH = 4;            // each warp owns an 8x4 pixel block of the tile
+constexpr int kBlocksX = kTile / kBlockW;          // 2 x 4 blocks
+static_assert(kBlockW * kBlockH == 32 && (kTile / kBlockW) * (kTile / kBlockH) == kWarps, "warp blocks");
+
+// Blocks of the tile (bit b = block (b % 2, b / 2)) that the quad of one record may touch: the
+// separating-axis test of two rectangles -- the block's rectangle of pixel centres against the quad,
+// on the block axes (the quad's axis-aligned extent from its rot_scale columns, widened by the same
+// 0.25-pixel margin the tile binning uses) and on the quad's own axes u and v (the rows of
+// rot_scale^-1 the blend evaluates, widened by a rounding margin far above the error of either
+// evaluation).  A cleared bit therefore means no pixel centre of the block is covered, and the
+// record changes none of its pixels.
+__device__ __forceinline__ u32 block_mask(const float4 q0, const float4 q1, const float4 q3, float ox, float oy,
+                                          float sx, float sy, float mx, float my) {
+  // ox, oy: NDC of the tile's first pixel centre; sx, sy: NDC step between pixel centres
+  const float hx = 0.5f * (kBlockW - 1) * sx, hy = 0.5f * (kBlockH - 1) * sy;  // block half extents
+  const float ex = 3.0f * (fabsf(q3.x) + fabsf(q3.z)) + mx + hx;
+  const float ey = 3.0f * (fabsf(q3.y) + fabsf(q3.w)) + my + hy;
+  const float au0 = fabsf(q0.z), au1 = fabsf(q0.w), av0 = fabsf(q1.x), av1 = fabsf(q1.y);
+  const float ru = au0 * hx + au1 * hy, rv = av0 * hx + av1 * hy;
+  u32 m = 0;
+#pragma unroll
+  for (int by = 0; by < kTile / kBlockH; ++by) {
+    const float dy = oy + (by * kBlockH + 0.5f * (kBlockH - 1)) * sy - q0.y;
+#pragma unroll
+    for (int bx = 0; bx < kBlocksX; ++bx) {
+      const float dx = ox + (bx * kBlockW + 0.5f * (kBlockW - 1)) * sx - q0.x;
+      const float u = q0.z * dx + q0.w * dy, v = q1.x * dx + q1.y * dy;
+      const float tu = 3.0f + ru + 4e-6f * (au0 * (fabsf(dx) + hx) + au1 * (fabsf(dy) + hy)) + 1e-3f;
+      const float tv = 3.0f + rv + 4e-6f * (av0 * (fabsf(dx) + hx) + av1 * (fabsf(dy) + hy)) + 1e-3f;
+      const bool hit = fabsf(dx) <= ex && fabsf(dy) <= ey && fabsf(u) <= tu && fabsf(v) <= tv;
+      m |= hit ? 1u << (by * kBlocksX + bx) : 0u;
+    }
+  }
+  return m;
+}
 
 template <bool DEPTH, bool COUNT>
 __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   __shared__ float4 s_q0[kRasterThreads];  // cx, cy, m00, m01
   __shared__ float4 s_q1[kRasterThreads];  // m10, m11, cz, opacity
   __shared__ float4 s_q2[kRasterThreads];  // r, g, b, -
+  __shared__ u32 s_bits[kWarps][kWarps];   // [block][32-record word]: records that may touch the block
   const u32 tile = blockIdx.x;
   const u32 tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-  const u32 tid = threadIdx.x;
-  const u32 px = tx * kTile + (tid % kTile), py = ty * kTile + (tid / kTile);
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const u32 px = tx * kTile + (warp % kBlocksX) * kBlockW + lane % kBlockW;
+  const u32 py = ty * kTile + (warp / kBlocksX) * kBlockH + lane / kBlockW;
   const bool inside = px < a.width && py < a.height;
   const float fx = __fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f;
   const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
   const float dpix = (DEPTH && inside) ? a.depth[(size_t)py * a.width + px] : 1.0f;
   const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range)[tile];
   const uint2 range = make_uint2(min(tr.x, a.pair_capacity), min(tr.y, a.pair_capacity));
+  // tile geometry for the block test
+  const float sx = 2.0f / (float)a.width, sy = 2.0f / (float)a.height;
+  const float ox = (float)(2 * tx * kTile + 1) / (float)a.width - 1.0f;
+  const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
+  const float mx = 0.5f * sx, my = 0.5f * sy;  // 0.25 pixel
 
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, ca = 0.0f;
   u32 frags = 0, needed = 0;
@@ -42,35 +87,51 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   for (u32 hi = range.y; hi > range.x;) {
     const u32 lo = (hi - range.x > (u32)kRasterThreads) ? hi - kRasterThreads : range.x;
     const u32 cnt = hi - lo;
+    u32 mask = 0;
     if (tid < cnt) {
       const u32 id = a.pair_splat[hi - 1 - tid];  // nearest first
       const float4* rec = a.record + 4 * (size_t)id;
-      s_q0[tid] = rec[0];
-      s_q1[tid] = rec[1];
+      const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
+      s_q0[tid] = q0;
+      s_q1[tid] = q1;
       s_q2[tid] = rec[2];
+      mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
+    }
+#pragma unroll
+    for (int b = 0; b < kWarps; ++b) {
+      const u32 bits = __ballot_sync(0xffffffffu, (mask >> b) & 1u);
+      if (lane == 0) s_bits[b][warp] = bits;
     }
     __syncthreads();
     if (!__all_sync(0xffffffffu, done)) {
-      for (u32 j = 0; j < cnt; ++j) {
-        const float4 q0 = s_q0[j], q1 = s_q1[j];
-        const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
-        const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
-        const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
-        bool cov = (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
-        if (DEPTH) cov &= q1.z < dpix;
-        if (COUNT) {
-          frags += (cov && inside) ? 1u : 0u;
-          needed += (cov && inside && T >= a.t_floor) ? 1u : 0u;
+      for (int k = 0; k < kWarps; ++k) {
+        u32 word = s_bits[warp][k];
+        while (word) {
+          const u32 j = 32u * k + (u32)(__ffs(word) - 1);
+          word &= word - 1u;
+          const float4 q0 = s_q0[j], q1 = s_q1[j];
+          const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
+          const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
+          const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
+          bool cov = (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
+          if (DEPTH) cov &= q1.z < dpix;
+          if (COUNT) {
+            frags += (cov && inside) ? 1u : 0u;
+            needed += (cov && inside && T >= a.t_floor) ? 1u : 0u;
+          }
+          const float g = exp2f(kExp * (u * u + v * v));
+          const float al = cov ? q1.w * g : 0.0f;
+          const float w = al * T;
+          const float4 q2 = s_q2[j];
+          cr += w * q2.x;
+          cg += w * q2.y;
+          cb += w * q2.z;
+          ca += w * al;
+          T -= w;
         }
-        const float g = exp2f(kExp * (u * u + v * v));
-        const float al = cov ? q1.w * g : 0.0f;
-        const float w = al * T;
-        const float4 q2 = s_q2[j];
-        cr += w * q2.x;
-        cg += w * q2.y;
-        cb += w * q2.z;
-        ca += w * al;
-        T -= w;
+        // A warp whose 32 pixels are all below t_floor stops here (the remaining records can move no
+        // channel of these pixels by more than t_floor).
+        if (!COUNT && __all_sync(0xffffffffu, done || T < a.t_floor)) break;
       }
     }
     hi = lo;
@@ -84,8 +145,8 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
       frags += __shfl_xor_sync(0xffffffffu, frags, o);
       needed += __shfl_xor_sync(0xffffffffu, needed, o);
     }
-    if ((tid & 31) == 0 && frags) atomicAdd(a.fragments, (unsigned long long)frags);
-    if ((tid & 31) == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
+    if (lane == 0 && frags) atomicAdd(a.fragments, (unsigned long long)frags);
+    if (lane == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
   }
   if (!inside) return;
   const size_t pix = (size_t)py * a.width + px;
