@@ -158,12 +158,14 @@ typedef struct gs_context_options {
 
 typedef struct gs_frame_stats {
   uint32_t visible_count;     /* V of the last frame */
-  uint32_t tile_pairs;        /* (splat, tile) pairs the last frame needed */
+  uint32_t tile_pairs;        /* largest (splat, tile) pair count of one depth slab of the last frame:
+                                 the max_tile_pairs capacity that frame needed */
   uint64_t fragments;         /* covered (pixel, splat) pairs passing the depth test: the fragment-shader
                                  invocations of the reference's draw; only with
                                  gs_context_set_count_fragments(1) */
   uint64_t fragments_blended; /* of those, the ones met front to back while the pixel's transmittance
                                  was still >= 2^-24 (the blend work actually needed) */
+  uint64_t pairs_emitted;     /* (splat, tile) pairs binned and sorted over all slabs of the last frame */
 } gs_frame_stats;
 
 /* Creates a context on the current CUDA device and reserves all scratch for the given capacities. */
@@ -175,6 +177,16 @@ gs_status gs_context_reserve(gs_context* context, const gs_context_options* opti
 
 /* Makes every following gs_render also count fragments (slower; for statistics and tests). */
 gs_status gs_context_set_count_fragments(gs_context* context, int enable);
+
+/* No counterpart in the reference (a scheduling knob of this implementation).  gs_render bins,
+ * sorts and blends the depth-sorted splats in up to GS_MAX_SLABS slabs, nearest first, carrying
+ * every pixel's blend state from one slab to the next; a 16x16 tile whose pixels all fall below
+ * transmittance 2^-24 is finished and receives no pairs from the slabs behind.  ends[i] is the
+ * cumulative share of the visible splats in slabs 0..i, in 1/1024 units, strictly increasing,
+ * with ends[count-1] = 1024; {1024} is a single slab.  The image is the same for every schedule up
+ * to the 2^-24 early stop. */
+#define GS_MAX_SLABS 4
+gs_status gs_context_set_slabs(gs_context* context, uint32_t count, const uint32_t* ends);
 
 /* One frame.  No allocation, no host synchronisation: safe to capture in a CUDA graph once the
  * context holds enough capacity. */

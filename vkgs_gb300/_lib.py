@@ -21,6 +21,7 @@ GS_ERROR_OUT_OF_MEMORY = 5
 GS_ERROR_INTERNAL = 6
 GS_NUM_STAGES = 6
 GS_SORT_NOALLOC_MAX_COUNT = 1 << 20  # include/vkgs_gb300.h
+GS_MAX_SLABS = 4
 STAGES = ("cull_project", "depth_sort", "bin", "tile_sort", "tile_ranges", "raster")
 
 
@@ -54,7 +55,7 @@ class GsContextOptions(ctypes.Structure):
 
 class GsFrameStats(ctypes.Structure):
     _fields_ = [("visible_count", c_uint32), ("tile_pairs", c_uint32), ("fragments", c_uint64),
-                ("fragments_blended", c_uint64)]
+                ("fragments_blended", c_uint64), ("pairs_emitted", c_uint64)]
 
 
 # (name, restype, argtypes) for every entry point of include/vkgs_gb300.h
@@ -72,6 +73,7 @@ SIGNATURES = [
     ("gs_context_destroy", None, [c_void_p]),
     ("gs_context_reserve", c_int, [c_void_p, POINTER(GsContextOptions)]),
     ("gs_context_set_count_fragments", c_int, [c_void_p, c_int]),
+    ("gs_context_set_slabs", c_int, [c_void_p, c_uint32, POINTER(c_uint32)]),
     ("gs_render", c_int,
      [c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), POINTER(GsFrameOutputs), c_void_p]),
     ("gs_context_check", c_int, [c_void_p, c_void_p, POINTER(GsFrameStats)]),

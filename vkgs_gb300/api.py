@@ -184,6 +184,13 @@ class Renderer:
         opts = L.GsContextOptions(int(max_splats), int(max_width), int(max_height), int(max_tile_pairs))
         _check(self._lib.gs_context_reserve(self._h, ctypes.byref(opts)), "gs_context_reserve")
 
+    def set_slabs(self, ends=(1024,)) -> None:
+        """Depth-slab schedule: cumulative shares of the visible splats (1/1024 units), nearest first,
+        ending at 1024.  (1024,) bins and sorts every splat in one pass."""
+        ends = [int(e) for e in ends]
+        arr = (ctypes.c_uint32 * len(ends))(*ends)
+        _check(self._lib.gs_context_set_slabs(self._h, len(ends), arr), "gs_context_set_slabs")
+
     def count_fragments(self, enable: bool = True) -> None:
         _check(self._lib.gs_context_set_count_fragments(self._h, int(bool(enable))), "count_fragments")
 
@@ -238,11 +245,13 @@ class Renderer:
         return np.frombuffer(buf, np.float32)[: got.value * L.GS_NUM_STAGES].reshape(-1, L.GS_NUM_STAGES).copy()
 
     def check(self, stream=None) -> dict:
-        """Synchronises and returns {visible_count, tile_pairs, fragments}; raises GsError on device errors."""
+        """Synchronises and returns {visible_count, tile_pairs, fragments, fragments_blended, pairs_emitted}
+        of the last frame; raises GsError on device errors."""
         st = L.GsFrameStats()
         status = self._lib.gs_context_check(self._h, _stream(stream), ctypes.byref(st))
         stats = {"visible_count": int(st.visible_count), "tile_pairs": int(st.tile_pairs),
-                 "fragments": int(st.fragments), "fragments_blended": int(st.fragments_blended)}
+                 "fragments": int(st.fragments), "fragments_blended": int(st.fragments_blended),
+                 "pairs_emitted": int(st.pairs_emitted)}
         if status != L.GS_SUCCESS:
             err = GsError(status, "gs_context_check")
             err.stats = stats

@@ -52,6 +52,9 @@ enum FrameWord : u32 {
   FW_PAIR_TOTAL = 2,
   FW_TICKET_CULL = 3,
   FW_FRAGMENTS = 4,  // u64 covered fragments at words 4..5, u64 blended fragments at 6..7
+  FW_SLAB_PAIRS = 8,  // pairs of the slab being binned
+  FW_PAIR_SUM = 10,   // u64 pairs over all slabs at words 10..11
+  FW_GIANTS = 12,     // giant-splat list length, one word per slab (12..15)
   FW_WORDS = 16,
 };
 
@@ -80,19 +83,28 @@ struct gs_context {
   size_t radix_status_words = 0;
   u32* bin_count = nullptr;
   u32* bin_block_sum = nullptr;
+  u32* giant_list = nullptr;
   u32* pair_tile = nullptr;
   u32* pair_splat = nullptr;
   u32* pair_tile_alt = nullptr;
   u32* pair_splat_alt = nullptr;
   u32* tile_range = nullptr;
+  u32* tile_done = nullptr;   // bitmap over tiles, cleared per frame
+  float4* state_c = nullptr;  // running pixel sums between depth slabs
+  float* state_t = nullptr;
+  u32 slab_count = 2;  // nearest eighth of the visible splats, then the rest
+  u32 slab_end[GS_MAX_SLABS] = {128, 1024, 1024, 1024};
   size_t status_bytes_begin = 0, status_bytes_end = 0;  // epoch-tagged region (zeroed on allocation)
-  // stage timing: a ring of kTimingRing frames x (GS_NUM_STAGES + 1) events
+  // stage timing: a ring of kTimingRing frames x kFrameEvents events -- start, after cull, after the
+  // depth sort, then per slab: after binning, tile sort, tile ranges and raster
   static constexpr u32 kTimingRing = 256;
+  static constexpr u32 kFrameEvents = 3 + 4 * GS_MAX_SLABS;
   bool timing = false;
   cudaEvent_t* events = nullptr;
+  u32 frame_slabs[kTimingRing] = {};
   u32 timed_frames = 0;  // frames recorded since enabling (may exceed the ring)
 
-  cudaEvent_t* frame_events(u32 frame) { return events + (size_t)(frame % kTimingRing) * (GS_NUM_STAGES + 1); }
+  cudaEvent_t* frame_events(u32 frame) { return events + (size_t)(frame % kTimingRing) * kFrameEvents; }
 
   u32 take_epochs(u32 k) {
     if (epoch > 0xffffff00u) {  // wrap: clear every epoch-tagged status word once
@@ -129,7 +141,11 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->inst_by_id = cv.take<float>((size_t)n * 12);
     t->bin_count = cv.take<u32>(n);
     t->bin_block_sum = cv.take<u32>(bin_block_sums(n));
+    t->giant_list = cv.take<u32>(n);
     t->tile_range = cv.take<u32>((size_t)max_tiles * 2);
+    t->tile_done = cv.take<u32>((max_tiles + 31) / 32);
+    t->state_c = cv.take<float4>((size_t)max_width * max_height);
+    t->state_t = cv.take<float>((size_t)max_width * max_height);
     t->radix_control = cv.take<u32>(kRadixControlBytes / sizeof(u32));
     t->pair_tile = cv.take<u32>(pairs);
     t->pair_splat = cv.take<u32>(pairs);
@@ -366,7 +382,7 @@ void gs_context_destroy(gs_context* c) {
     cudaFree(c->arena);
   }
   if (c->events) {
-    for (u32 i = 0; i < gs_context::kTimingRing * (GS_NUM_STAGES + 1); ++i) cudaEventDestroy(c->events[i]);
+    for (u32 i = 0; i < gs_context::kTimingRing * gs_context::kFrameEvents; ++i) cudaEventDestroy(c->events[i]);
     delete[] c->events;
   }
   delete c;
@@ -375,7 +391,7 @@ void gs_context_destroy(gs_context* c) {
 gs_status gs_context_enable_timing(gs_context* c, int enable) {
   if (!c) return GS_ERROR_INVALID_ARGUMENT;
   if (enable && !c->events) {
-    const u32 total = gs_context::kTimingRing * (GS_NUM_STAGES + 1);
+    const u32 total = gs_context::kTimingRing * gs_context::kFrameEvents;
     c->events = new (std::nothrow) cudaEvent_t[total];
     if (!c->events) return GS_ERROR_OUT_OF_MEMORY;
     for (u32 i = 0; i < total; ++i) {
@@ -402,10 +418,20 @@ gs_status gs_context_stage_times(gs_context* c, uint32_t max_frames, float* ms, 
   const u32 first = c->timed_frames - kept;
   for (u32 r = 0; r < rows; ++r) {
     cudaEvent_t* ev = c->frame_events(first + r);
-    for (int s = 0; s < GS_NUM_STAGES; ++s) {
+    const u32 slabs = c->frame_slabs[(first + r) % gs_context::kTimingRing];
+    float* row = ms + (size_t)r * GS_NUM_STAGES;
+    for (int s = 0; s < GS_NUM_STAGES; ++s) row[s] = 0.0f;
+    auto add = [&](int stage, int e0, int e1) {
       float t = 0.0f;
-      if (cudaEventElapsedTime(&t, ev[s], ev[s + 1]) != cudaSuccess) return GS_ERROR_CUDA;
-      ms[(size_t)r * GS_NUM_STAGES + s] = t;
+      if (cudaEventElapsedTime(&t, ev[e0], ev[e1]) != cudaSuccess) return false;
+      row[stage] += t;
+      return true;
+    };
+    if (!add(0, 0, 1) || !add(1, 1, 2)) return GS_ERROR_CUDA;
+    for (u32 k = 0; k < slabs; ++k) {  // stages 2..5 summed over the slabs
+      const int b = 3 + 4 * (int)k, prev = k ? b - 1 : 2;
+      if (!add(2, prev, b) || !add(3, b, b + 1) || !add(4, b + 1, b + 2) || !add(5, b + 2, b + 3))
+        return GS_ERROR_CUDA;
     }
   }
   *frames = rows;
@@ -422,6 +448,16 @@ gs_status gs_context_reserve(gs_context* c, const gs_context_options* o) {
   if (n == c->max_splats && w == c->max_width && h == c->max_height && pairs == c->pair_capacity) return GS_SUCCESS;
   if (cudaDeviceSynchronize() != cudaSuccess) return GS_ERROR_CUDA;
   return context_allocate(c, n, w, h, pairs);
+}
+
+gs_status gs_context_set_slabs(gs_context* c, uint32_t count, const uint32_t* ends) {
+  if (!c || !ends || count == 0 || count > GS_MAX_SLABS) return GS_ERROR_INVALID_ARGUMENT;
+  for (u32 i = 0; i < count; ++i)
+    if (ends[i] == 0 || ends[i] > 1024 || (i && ends[i] <= ends[i - 1])) return GS_ERROR_INVALID_ARGUMENT;
+  if (ends[count - 1] != 1024) return GS_ERROR_INVALID_ARGUMENT;
+  c->slab_count = count;
+  for (u32 i = 0; i < GS_MAX_SLABS; ++i) c->slab_end[i] = i < count ? ends[i] : 1024;
+  return GS_SUCCESS;
 }
 
 gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
@@ -460,7 +496,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   if (ev) GS_TRY(cudaEventRecord(ev[i], st))
   GS_MARK(0);
   GS_TRY(cudaMemsetAsync(c->frame, 0, FW_WORDS * sizeof(u32), st));
-  GS_TRY(cudaMemsetAsync(c->tile_range, 0, (size_t)tiles * 2 * sizeof(u32), st));
+  GS_TRY(cudaMemsetAsync(c->tile_done, 0, (size_t)(tiles + 31) / 32 * sizeof(u32), st));
   u32* key = o.keys ? o.keys : c->key;
   u32* index = o.index ? o.index : c->index;
   const bool want_inst = o.instances != nullptr;
@@ -505,74 +541,94 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     GS_TRY(launch_instances(index, c->frame + FW_VISIBLE, c->inst_by_id, n, o.instances, o.draw_indirect, st));
   GS_MARK(2);
 
-  BinArgs ba{};
-  ba.index = index;
-  ba.visible_count = c->frame + FW_VISIBLE;
-  ba.record = c->record;
-  ba.n = n;
-  ba.width = W;
-  ba.height = H;
-  ba.tiles_x = tiles_x;
-  ba.tiles_y = tiles_y;
-  ba.count = c->bin_count;
-  ba.block_sum = c->bin_block_sum;
-  ba.pair_tile = c->pair_tile;
-  ba.pair_splat = c->pair_splat;
-  ba.pair_capacity = c->pair_capacity;
-  ba.pair_count = c->frame + FW_PAIR_COUNT;
-  ba.pair_total = c->frame + FW_PAIR_TOTAL;
-  ba.err = c->err;
-  GS_TRY(launch_bin(ba, st, nullptr, nullptr, c->num_sms));
-  GS_MARK(3);
-
-  // Stable sort of the pairs by tile id alone: each tile's list keeps the sorted (draw) order.
-  const u32* sorted_tile = c->pair_tile;
-  const u32* sorted_splat = c->pair_splat;
+  // Depth slabs, nearest first (one slab when nothing is visible).
+  const u32 slabs = n > 0 ? c->slab_count : 1;
+  if (ev) c->frame_slabs[(c->timed_frames - 1) % gs_context::kTimingRing] = slabs;
   u32 tile_bits = 0;
   while (tile_bits < 32 && (1ull << tile_bits) < tiles) ++tile_bits;
-  if (n > 0 && tile_bits > 0) {
-    RadixSortArgs ra{};
-    ra.keys = c->pair_tile;
-    ra.values = c->pair_splat;
-    ra.keys_alt = c->pair_tile_alt;
-    ra.values_alt = c->pair_splat_alt;
-    ra.count = c->frame + FW_PAIR_COUNT;
-    ra.max_count = c->pair_capacity;
-    ra.begin_bit = 0;
-    ra.end_bit = tile_bits;
-    ra.control = c->radix_control;
-    ra.status = c->radix_status;
-    const u32 passes = radix_passes(0, tile_bits);
-    ra.epoch = c->take_epochs(passes);
-    ra.err = c->err;
-    ra.num_sms = c->num_sms;
-    GS_TRY(radix_sort(ra, st));
-    if (passes & 1u) {
-      sorted_tile = c->pair_tile_alt;
-      sorted_splat = c->pair_splat_alt;
-    }
-  }
-  GS_MARK(4);
-  if (n > 0)
-    GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range, c->num_sms, st));
+  for (u32 k = 0; k < slabs; ++k) {
+    const int e = 3 + 4 * (int)k;
+    GS_TRY(cudaMemsetAsync(c->tile_range, 0, (size_t)tiles * 2 * sizeof(u32), st));
+    BinArgs ba{};
+    ba.index = index;
+    ba.visible_count = c->frame + FW_VISIBLE;
+    ba.record = c->record;
+    ba.n = n;
+    ba.slab_e0 = k ? c->slab_end[k - 1] : 0;
+    ba.slab_e1 = slabs == 1 ? 1024 : c->slab_end[k];
+    ba.tile_done = k ? c->tile_done : nullptr;
+    ba.width = W;
+    ba.height = H;
+    ba.tiles_x = tiles_x;
+    ba.tiles_y = tiles_y;
+    ba.count = c->bin_count;
+    ba.block_sum = c->bin_block_sum;
+    ba.giant_list = c->giant_list;
+    ba.giant_count = c->frame + FW_GIANTS + k;
+    ba.pair_tile = c->pair_tile;
+    ba.pair_splat = c->pair_splat;
+    ba.pair_capacity = c->pair_capacity;
+    ba.pair_count = c->frame + FW_PAIR_COUNT;
+    ba.slab_pairs = c->frame + FW_SLAB_PAIRS;
+    ba.pair_total = c->frame + FW_PAIR_TOTAL;
+    ba.pair_sum = reinterpret_cast<unsigned long long*>(c->frame + FW_PAIR_SUM);
+    ba.err = c->err;
+    GS_TRY(launch_bin(ba, st, nullptr, nullptr, c->num_sms));
+    GS_MARK(e);
 
-  RasterArgs rr{};
-  rr.tile_range = c->tile_range;
-  rr.pair_capacity = c->pair_capacity;
-  rr.pair_splat = sorted_splat;
-  rr.record = c->record;
-  rr.width = W;
-  rr.height = H;
-  rr.tiles_x = tiles_x;
-  rr.tiles_y = tiles_y;
-  rr.out_rgba = t->color_rgba32f;
-  rr.out_bgra = reinterpret_cast<uchar4*>(t->color_bgra8);
-  rr.depth = t->depth;
-  rr.t_floor = 5.9604645e-08f;  // 2^-24
-  rr.fragments = c->count_fragments ? reinterpret_cast<unsigned long long*>(c->frame + FW_FRAGMENTS) : nullptr;
-  GS_MARK(5);
-  GS_TRY(launch_raster(rr, st));
-  GS_MARK(6);
+    // Stable sort of the slab's pairs by tile id alone: each tile's list keeps the draw order.
+    const u32* sorted_tile = c->pair_tile;
+    const u32* sorted_splat = c->pair_splat;
+    if (n > 0 && tile_bits > 0) {
+      RadixSortArgs ra{};
+      ra.keys = c->pair_tile;
+      ra.values = c->pair_splat;
+      ra.keys_alt = c->pair_tile_alt;
+      ra.values_alt = c->pair_splat_alt;
+      ra.count = c->frame + FW_PAIR_COUNT;
+      ra.max_count = c->pair_capacity;
+      ra.begin_bit = 0;
+      ra.end_bit = tile_bits;
+      ra.control = c->radix_control;
+      ra.status = c->radix_status;
+      const u32 passes = radix_passes(0, tile_bits);
+      ra.epoch = c->take_epochs(passes);
+      ra.err = c->err;
+      ra.num_sms = c->num_sms;
+      GS_TRY(radix_sort(ra, st));
+      if (passes & 1u) {
+        sorted_tile = c->pair_tile_alt;
+        sorted_splat = c->pair_splat_alt;
+      }
+    }
+    GS_MARK(e + 1);
+    if (n > 0)
+      GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range, c->num_sms,
+                                st));
+    GS_MARK(e + 2);
+
+    RasterArgs rr{};
+    rr.tile_range = c->tile_range;
+    rr.pair_capacity = c->pair_capacity;
+    rr.pair_splat = sorted_splat;
+    rr.record = c->record;
+    rr.width = W;
+    rr.height = H;
+    rr.tiles_x = tiles_x;
+    rr.tiles_y = tiles_y;
+    rr.out_rgba = t->color_rgba32f;
+    rr.out_bgra = reinterpret_cast<uchar4*>(t->color_bgra8);
+    rr.depth = t->depth;
+    rr.t_floor = 5.9604645e-08f;  // 2^-24
+    rr.fragments = c->count_fragments ? reinterpret_cast<unsigned long long*>(c->frame + FW_FRAGMENTS) : nullptr;
+    rr.state_c = c->state_c;
+    rr.state_t = c->state_t;
+    rr.tile_done = c->tile_done;
+    rr.first = k == 0;
+    rr.last = k + 1 == slabs;
+    GS_TRY(launch_raster(rr, st));
+    GS_MARK(e + 3);
+  }
 
   if (o.visible_count)
     GS_TRY(cudaMemcpyAsync(o.visible_count, c->frame + FW_VISIBLE, sizeof(u32), cudaMemcpyDeviceToDevice, st));
@@ -593,6 +649,9 @@ gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stat
   if (stats) {
     stats->visible_count = words[FW_VISIBLE];
     stats->tile_pairs = words[FW_PAIR_TOTAL];
+    uint64_t ps;
+    std::memcpy(&ps, words + FW_PAIR_SUM, 8);
+    stats->pairs_emitted = ps;
     uint64_t f[2];
     std::memcpy(f, words + FW_FRAGMENTS, 16);
     stats->fragments = f[0];

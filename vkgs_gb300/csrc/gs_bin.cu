@@ -11,6 +11,8 @@
 //              thousands of tiles is spread over the whole warp
 //   4. a stable radix sort on the tile id alone (gs_sort.cu) then groups them by tile without
 //      disturbing that order, and tile ranges are read off the sorted tile ids.
+// Everything runs over one depth slab of the sorted splats at a time (sorted positions [lo, hi)); from
+// the second slab on, tiles that an earlier slab finished (tile_done bitmap) receive no pairs.
 // The tile test is exact up to a small margin: the quad (corners c +- a +- b) is clipped to each tile
 // row's band of pixel centres and the tile columns its x-extent reaches are taken; the margin only
 // ever adds pairs.  count and emit evaluate the same footprint arithmetic (this unit is compiled
@@ -27,6 +29,9 @@ constexpr u32 kScanThreads = 256;
 constexpr u32 kScanItems = 16;
 constexpr u32 kScanTile = kScanThreads * kScanItems;  // counts per scan block
 constexpr float kMarginPx = 0.25f;
+constexpr u32 kGiantPairs = 128;    // splats with more pairs are expanded by a whole CTA (k_bin_giants)
+constexpr u32 kGiantThreads = 256;
+constexpr u32 kGiantRows = 1024;    // row prefix held in shared memory per pass
 
 // The quad of one splat prepared for row clipping: corners in order and inverse edge slopes.
 struct Footprint {
@@ -126,30 +131,65 @@ __device__ __forceinline__ u32 footprint_pairs(const Footprint& f, const TargetG
   return n;
 }
 
-__device__ __forceinline__ u32 visible(const BinArgs& a) { return min(*a.visible_count, a.n); }
+// Set bits of the done bitmap over tile ids [t0, t1].
+__device__ __forceinline__ u32 done_in_range(const u32* __restrict__ done, u32 t0, u32 t1) {
+  u32 n = 0;
+  for (u32 w = t0 >> 5; w <= (t1 >> 5); ++w) {
+    u32 bits = __ldg(done + w);
+    if (w == (t0 >> 5)) bits &= 0xffffffffu << (t0 & 31u);
+    if (w == (t1 >> 5)) bits &= 0xffffffffu >> (31u - (t1 & 31u));
+    n += __popc(bits);
+  }
+  return n;
+}
+
+__device__ __forceinline__ bool tile_is_done(const u32* __restrict__ done, u32 t) {
+  return (__ldg(done + (t >> 5)) >> (t & 31u)) & 1u;
+}
+
+// pairs of the footprint whose tile is not finished
+__device__ __forceinline__ u32 footprint_open_pairs(const Footprint& f, const TargetGeom& g, const u32* done) {
+  u32 n = 0;
+  for (int ty = f.ty0; ty <= f.ty1; ++ty) {
+    int tx0, tx1;
+    footprint_cols(f, g, ty, tx0, tx1);
+    if (tx1 < tx0) continue;
+    const u32 base = (u32)ty * g.tiles_x;
+    n += (u32)(tx1 - tx0 + 1) - done_in_range(done, base + (u32)tx0, base + (u32)tx1);
+  }
+  return n;
+}
+
+__device__ __forceinline__ SlabBounds slab(const BinArgs& a) {
+  return slab_bounds(min(*a.visible_count, a.n), a.slab_e0, a.slab_e1);
+}
 
 // 1. pairs per sorted splat
 __global__ __launch_bounds__(kCountThreads) void k_bin_count(const BinArgs a) {
-  const u32 v = visible(a);
+  const SlabBounds sb = slab(a);
   const TargetGeom g = target_geom(a);
   const u32 stride = gridDim.x * blockDim.x;
-  for (u32 r = blockIdx.x * blockDim.x + threadIdx.x; r < v; r += stride) {
+  for (u32 r = sb.lo + blockIdx.x * blockDim.x + threadIdx.x; r < sb.hi; r += stride) {
     Footprint f;
-    a.count[r] = footprint(a.record, __ldg(a.index + r), g, f) ? footprint_pairs(f, g) : 0u;
+    u32 c = 0;
+    if (footprint(a.record, __ldg(a.index + r), g, f))
+      c = a.tile_done ? footprint_open_pairs(f, g, a.tile_done) : footprint_pairs(f, g);
+    a.count[r] = c;
+    if (c > kGiantPairs) a.giant_list[atomicAdd(a.giant_count, 1u)] = r;
   }
 }
 
 // 2a. per-block sums of count[]
 __global__ __launch_bounds__(kScanThreads) void k_bin_reduce(const BinArgs a) {
   __shared__ u32 s_scan[32];
-  const u32 v = visible(a);
-  const u32 base = blockIdx.x * kScanTile;
-  if (base >= v) return;
+  const SlabBounds sb = slab(a);
+  const u32 base = sb.lo + blockIdx.x * kScanTile;
+  if (base >= sb.hi) return;
   u32 s = 0;
 #pragma unroll
   for (u32 i = 0; i < kScanItems; ++i) {
     const u32 r = base + i * kScanThreads + threadIdx.x;
-    s += r < v ? a.count[r] : 0u;
+    s += r < sb.hi ? a.count[r] : 0u;
   }
   u32 total;
   block_exclusive_scan<kScanThreads>(s, s_scan, &total);
@@ -160,7 +200,8 @@ __global__ __launch_bounds__(kScanThreads) void k_bin_reduce(const BinArgs a) {
 __global__ __launch_bounds__(1024) void k_bin_scan_blocks(const BinArgs a) {
   __shared__ u32 s_scan[32];
   __shared__ u32 s_carry;
-  const u32 nblocks = (visible(a) + kScanTile - 1) / kScanTile;
+  const SlabBounds sb = slab(a);
+  const u32 nblocks = (sb.hi - sb.lo + kScanTile - 1) / kScanTile;
   if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
   for (u32 b0 = 0; b0 < nblocks; b0 += 1024) {
@@ -175,8 +216,10 @@ __global__ __launch_bounds__(1024) void k_bin_scan_blocks(const BinArgs a) {
   }
   if (threadIdx.x == 0) {
     const u32 P = s_carry;
-    *a.pair_total = P;
+    *a.slab_pairs = P;
     *a.pair_count = min(P, a.pair_capacity);
+    atomicMax(a.pair_total, P);
+    *a.pair_sum += P;
     if (P > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
   }
 }
@@ -185,13 +228,13 @@ __global__ __launch_bounds__(1024) void k_bin_scan_blocks(const BinArgs a) {
 __global__ __launch_bounds__(kScanThreads) void k_bin_scan(const BinArgs a) {
   __shared__ u32 s_scan[32];
   __shared__ u32 s_vals[kScanTile];
-  const u32 v = visible(a);
-  const u32 base = blockIdx.x * kScanTile;
-  if (base >= v) return;
+  const SlabBounds sb = slab(a);
+  const u32 base = sb.lo + blockIdx.x * kScanTile;
+  if (base >= sb.hi) return;
   // blocked arrangement: thread t owns elements [t*items, (t+1)*items) of the block
   for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
     const u32 r = base + i;
-    s_vals[i] = r < v ? a.count[r] : 0u;
+    s_vals[i] = r < sb.hi ? a.count[r] : 0u;
   }
   __syncthreads();
   u32 x[kScanItems], s = 0;
@@ -210,7 +253,7 @@ __global__ __launch_bounds__(kScanThreads) void k_bin_scan(const BinArgs a) {
   __syncthreads();
   for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
     const u32 r = base + i;
-    if (r < v) a.count[r] = s_vals[i];
+    if (r < sb.hi) a.count[r] = s_vals[i];
   }
 }
 
@@ -300,36 +343,133 @@ __device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const 
 }
 
 // 3. emission: warp w walks 32 consecutive sorted splats' pairs -- splat by splat, row-major inside a
-//    splat -- with the span list of for_each_pair, and stores them coalesced into their contiguous
-//    output range [first[r0], ...): pairs leave in ascending sorted position.
+//    splat -- with the span list of for_each_pair, drops pairs of finished tiles, and stores the rest
+//    coalesced into the group's contiguous output range [first[r0], ...): pairs leave in ascending
+//    sorted position.
 __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
   __shared__ u32 s_spans[kEmitWarps][2 * (kSpanBuf + 1)];
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const u32 v = visible(a);
-  const u32 P = *a.pair_total;
+  const SlabBounds sb = slab(a);
+  const u32 P = *a.slab_pairs;
   const TargetGeom g = target_geom(a);
   const u32 gwarps = gridDim.x * kEmitWarps;
-  for (u32 r0 = (blockIdx.x * kEmitWarps + warp) * 32; r0 < v; r0 += gwarps * 32) {
+  const u32 lt = lanemask_lt();
+  for (u32 r0 = sb.lo + (blockIdx.x * kEmitWarps + warp) * 32; r0 < sb.hi; r0 += gwarps * 32) {
+    const u32 gfirst = a.count[r0];  // exclusive prefix after the scan
+    const u32 rl = min(r0 + 32u, sb.hi);
+    const u32 gend = rl < sb.hi ? a.count[rl] : P;
+    if (gfirst == gend) continue;  // no open pair in this group (warp-uniform)
     const u32 r = r0 + lane;
     Footprint f;
     bool ok = false;
-    u32 id = 0;
-    if (r < v) {
-      id = __ldg(a.index + r);
-      ok = footprint(a.record, id, g, f);
+    u32 id = 0, giant = 0;
+    if (r < sb.hi) {
+      const u32 mine = (r + 1 < sb.hi ? a.count[r + 1] : P) - a.count[r];
+      if (mine > kGiantPairs) {
+        giant = mine;  // k_bin_giants writes these
+      } else {
+        id = __ldg(a.index + r);
+        ok = footprint(a.record, id, g, f);
+      }
     }
-    const u32 gfirst = a.count[r0];  // exclusive prefix after the scan
-    const u32 rl = min(r0 + 32u, v);
-    const u32 gend = rl < v ? a.count[rl] : P;
-    const u32 total = for_each_pair(f, ok, g, s_spans[warp], [&](bool has, u32 tile, u32 owner, u32 j) {
+    // giant pairs of the lanes before this one: the gaps their ranges leave in the group's output
+    u32 gincl = giant;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 y = __shfl_up_sync(0xffffffffu, gincl, o);
+      if (lane >= (u32)o) gincl += y;
+    }
+    const u32 gexcl = gincl - giant, gtotal = __shfl_sync(0xffffffffu, gincl, 31);
+    u32 kept = 0;  // pairs of non-giant splats written so far
+    for_each_pair(f, ok, g, s_spans[warp], [&](bool has, u32 tile, u32 owner, u32) {
       const u32 oid = __shfl_sync(0xffffffffu, id, owner);
-      const u32 pos = gfirst + j;
-      if (has && pos < a.pair_capacity) {
+      const u32 gap = __shfl_sync(0xffffffffu, gexcl, owner);
+      const bool keep = has && !(a.tile_done && tile_is_done(a.tile_done, tile));
+      const u32 ballot = __ballot_sync(0xffffffffu, keep);
+      const u32 pos = gfirst + gap + kept + __popc(ballot & lt);
+      if (keep && pos < a.pair_capacity) {
         a.pair_tile[pos] = tile;
         a.pair_splat[pos] = oid;
       }
+      kept += __popc(ballot);
     });
-    if (lane == 0 && gfirst + total != gend) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
+    if (lane == 0 && gfirst + gtotal + kept != gend) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
+  }
+}
+
+// 3b. giants: one CTA per splat with more than kGiantPairs pairs.  Its rows' spans are listed in
+//     shared memory with a block-wide prefix, every thread takes pairs j = tid, tid + 256, ... and
+//     finds its row by binary search, and open pairs are packed into the splat's output range (the
+//     order inside one splat's range is free: a splat meets each tile once, and the stable tile sort
+//     only orders pairs of different splats).
+__global__ __launch_bounds__(kGiantThreads) void k_bin_giants(const BinArgs a) {
+  __shared__ u32 s_pfx[kGiantRows + 1];
+  __shared__ u32 s_base[kGiantRows];
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_cursor;
+  const SlabBounds sb = slab(a);
+  const u32 P = *a.slab_pairs;
+  const u32 ng = *a.giant_count;
+  const TargetGeom g = target_geom(a);
+  const u32 tid = threadIdx.x, lane = tid & 31u;
+  for (u32 k = blockIdx.x; k < ng; k += gridDim.x) {
+    const u32 r = a.giant_list[k];
+    const u32 first = a.count[r];
+    const u32 end = r + 1 < sb.hi ? a.count[r + 1] : P;
+    Footprint f;
+    const u32 id = __ldg(a.index + r);
+    footprint(a.record, id, g, f);
+    if (tid == 0) s_cursor = 0;
+    const u32 nrows = (u32)max(0, f.ty1 - f.ty0 + 1);
+    for (u32 w0 = 0; w0 < nrows; w0 += kGiantRows) {  // windows of rows (one for any real target)
+      const u32 m = min(kGiantRows, nrows - w0);
+      u32 carry = 0;
+      for (u32 i0 = 0; i0 < m; i0 += kGiantThreads) {
+        const u32 i = i0 + tid;
+        u32 width = 0;
+        if (i < m) {
+          const int ty = f.ty0 + (int)(w0 + i);
+          int tx0, tx1;
+          footprint_cols(f, g, ty, tx0, tx1);
+          width = (u32)max(0, tx1 - tx0 + 1);
+          s_base[i] = (u32)ty * g.tiles_x + (u32)max(tx0, 0);
+        }
+        u32 tot;
+        const u32 ex = block_exclusive_scan<kGiantThreads>(width, s_scan, &tot);
+        if (i < m) s_pfx[i] = carry + ex;
+        carry += tot;
+        __syncthreads();
+      }
+      if (tid == 0) s_pfx[m] = carry;
+      __syncthreads();
+      for (u32 j0 = 0; j0 < carry; j0 += kGiantThreads) {
+        const u32 j = j0 + tid;
+        bool keep = false;
+        u32 tile = 0;
+        if (j < carry) {
+          u32 lo = 0, hi = m;  // last row with s_pfx[row] <= j
+          while (hi - lo > 1) {
+            const u32 mid = (lo + hi) >> 1;
+            if (s_pfx[mid] <= j) lo = mid;
+            else hi = mid;
+          }
+          tile = s_base[lo] + (j - s_pfx[lo]);
+          keep = !(a.tile_done && tile_is_done(a.tile_done, tile));
+        }
+        const u32 ballot = __ballot_sync(0xffffffffu, keep);
+        u32 wbase = 0;
+        if (lane == 0 && ballot) wbase = atomicAdd(&s_cursor, (u32)__popc(ballot));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        const u32 pos = first + wbase + __popc(ballot & lanemask_lt());
+        if (keep && pos < end && pos < a.pair_capacity) {
+          a.pair_tile[pos] = tile;
+          a.pair_splat[pos] = id;
+        }
+      }
+      __syncthreads();
+    }
+    if (tid == 0 && s_cursor != end - first) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
+    __syncthreads();
   }
 }
 
@@ -365,6 +505,7 @@ cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_
   if (after_scan) cudaEventRecord(after_scan, stream);
   const u32 emit_grid = min((a.n + kEmitThreads - 1) / kEmitThreads, sms * 8u);
   k_bin_emit<<<emit_grid, kEmitThreads, 0, stream>>>(a);
+  k_bin_giants<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

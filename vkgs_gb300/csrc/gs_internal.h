@@ -66,19 +66,35 @@ cudaError_t launch_instances(const u32* index, const u32* visible_count, const f
 constexpr u32 kTile = 16;            // tile edge in pixels
 constexpr u32 kMaxTiles = 1u << 24;  // tile ids must stay below 2^24 (radix passes on the tile id)
 
+// Sorted positions [lo, hi) of one depth slab: ends e_prev < e_cur are cumulative shares of V in
+// 1/1024 units counted from the nearest splat (the end of the ascending sort).
+struct SlabBounds {
+  u32 lo, hi;
+};
+__host__ __device__ inline SlabBounds slab_bounds(u32 v, u32 e_prev, u32 e_cur) {
+  const auto off = [v](u32 e) { return (u32)(((unsigned long long)v * e + 1023ull) >> 10); };
+  return SlabBounds{v - off(e_cur), v - off(e_prev)};
+}
+
 struct BinArgs {
   const u32* index;          // sorted splat ids
   const u32* visible_count;
   const float4* record;
   u32 n;                     // launch bound for V
+  u32 slab_e0, slab_e1;      // this slab's share of V (slab_bounds)
+  const u32* tile_done;      // bitmap of finished tiles (they get no pairs), or null
   u32 width, height, tiles_x, tiles_y;
   u32* count;                // [n] pairs per sorted splat, then its first pair (exclusive prefix)
   u32* block_sum;            // [bin_block_sums(n)]
   u32* pair_tile;            // out: tile id per pair, pairs in sorted-splat order
   u32* pair_splat;           // out: splat id per pair
   u32 pair_capacity;
-  u32* pair_count;           // out: min(total, capacity)
-  u32* pair_total;           // out: pairs needed
+  u32* giant_list;           // [n] sorted positions of splats with more than kGiantPairs pairs
+  u32* giant_count;          // this slab's entries in giant_list (zeroed before the slab)
+  u32* pair_count;           // out: min(slab pairs, capacity)
+  u32* slab_pairs;           // out: pairs this slab needs
+  u32* pair_total;           // out: max over the frame's slabs (atomicMax)
+  unsigned long long* pair_sum;  // out: sum over the frame's slabs
   u32* err;
 };
 
@@ -100,6 +116,10 @@ struct RasterArgs {
   uchar4* out_bgra;          // may be null
   const float* depth;        // may be null
   float t_floor;             // blending stops once every pixel of a tile is below this transmittance
+  float4* state_c;           // [H*W] running (r, g, b, a) between slabs
+  float* state_t;            // [H*W] running transmittance between slabs
+  u32* tile_done;            // bitmap: tiles finished by an earlier slab (set here when one finishes)
+  int first, last;           // first slab: no state to load; last slab: every tile resolves
   unsigned long long* fragments;  // non-null: [0] covered fragments, [1] those met while T >= t_floor
                                   // (disables the early stop)
 };

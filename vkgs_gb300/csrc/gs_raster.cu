@@ -13,7 +13,10 @@
 // the restatement's.  Each warp owns an 8x4 pixel block and walks only the records whose quad can
 // reach that block (a conservative per-batch test), which leaves every pixel's sum unchanged.  A warp
 // stops once its pixels' transmittance is below t_floor, and the tile once all its pixels are: the
-// splats behind can then change no channel by more than t_floor.
+// splats behind can then change no channel by more than t_floor.  The sorted splats arrive in depth
+// slabs, nearest first: a tile that is not finished stores its pixels' running sums for the next
+// slab's launch, a finished one writes its pixels and is marked done (later slabs skip it), and the
+// last slab writes every remaining tile.
 #include "gs_common.cuh"
 #include "gs_internal.h"
 
@@ -64,6 +67,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   __shared__ float4 s_q2[kRasterThreads];  // r, g, b, -
   __shared__ u32 s_bits[kWarps][kWarps];   // [block][32-record word]: records that may touch the block
   const u32 tile = blockIdx.x;
+  if (!a.first && ((a.tile_done[tile >> 5] >> (tile & 31u)) & 1u)) return;  // finished by an earlier slab
   const u32 tx = tile % a.tiles_x, ty = tile / a.tiles_x;
   const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const u32 px = tx * kTile + (warp % kBlocksX) * kBlockW + lane % kBlockW;
@@ -80,10 +84,16 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
   const float mx = 0.5f * sx, my = 0.5f * sy;  // 0.25 pixel
 
+  const size_t pix = (size_t)py * a.width + px;
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f, ca = 0.0f;
+  if (!a.first && inside) {  // the running sums of the nearer slabs
+    const float4 c = a.state_c[pix];
+    cr = c.x, cg = c.y, cb = c.z, ca = c.w;
+    T = a.state_t[pix];
+  }
   u32 frags = 0, needed = 0;
   const float kExp = -0.5f * 1.4426950408889634f;  // -log2(e)/2
-  bool done = !inside;
+  bool done = !inside || (!COUNT && T < a.t_floor);
   for (u32 hi = range.y; hi > range.x;) {
     const u32 lo = (hi - range.x > (u32)kRasterThreads) ? hi - kRasterThreads : range.x;
     const u32 cnt = hi - lo;
@@ -139,6 +149,9 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
     // Barrier before the next batch overwrites shared memory; also ends the tile once all are done.
     if (__syncthreads_and(done)) break;
   }
+  // Finished: every pixel below t_floor (never while counting, which disables the early stop).
+  const bool finished = __syncthreads_and(done);
+  if (finished && !a.last && tid == 0) atomicOr(a.tile_done + (tile >> 5), 1u << (tile & 31u));
   if (COUNT) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -149,7 +162,11 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
     if (lane == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
   }
   if (!inside) return;
-  const size_t pix = (size_t)py * a.width + px;
+  if (!finished && !a.last) {  // a farther slab continues these pixels
+    a.state_c[pix] = make_float4(cr, cg, cb, ca);
+    a.state_t[pix] = T;
+    return;
+  }
   const float alpha = ca + T;
   if (a.out_rgba) reinterpret_cast<float4*>(a.out_rgba)[pix] = make_float4(cr, cg, cb, alpha);
   if (a.out_bgra) {
