@@ -196,7 +196,8 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,
- * (splat, tile) pair count/scan/emission, stable tile sort of the pairs, tile ranges, raster + blend. */
+ * per-tile pair count + scan, pair emission into tile segments, per-tile sort by draw order,
+ * raster + blend; the last four are summed over the frame's depth slabs. */
 #define GS_NUM_STAGES 6
 gs_status gs_context_enable_timing(gs_context* context, int enable);
 

@@ -82,14 +82,13 @@ struct gs_context {
   u64* radix_status = nullptr;
   size_t radix_status_words = 0;
   u32* bin_count = nullptr;
-  u32* bin_block_sum = nullptr;
+  u32* bin_diff = nullptr;
   u32* giant_list = nullptr;
-  u32* pair_tile = nullptr;
+  u32* pair_key = nullptr;
   u32* pair_splat = nullptr;
-  u32* pair_tile_alt = nullptr;
-  u32* pair_splat_alt = nullptr;
   u32* tile_range = nullptr;
   u32* tile_done = nullptr;   // bitmap over tiles, cleared per frame
+  u32* tile_order = nullptr;
   float4* state_c = nullptr;  // running pixel sums between depth slabs
   float* state_t = nullptr;
   u32 slab_count = 2;  // nearest eighth of the visible splats, then the rest
@@ -140,20 +139,19 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->record = cv.take<float4>((size_t)n * 4);
     t->inst_by_id = cv.take<float>((size_t)n * 12);
     t->bin_count = cv.take<u32>(n);
-    t->bin_block_sum = cv.take<u32>(bin_block_sums(n));
+    t->bin_diff = cv.take<u32>(bin_diff_words(tiles_x, tiles_y));
     t->giant_list = cv.take<u32>(n);
-    t->tile_range = cv.take<u32>((size_t)max_tiles * 2);
+    t->tile_range = cv.take<u32>((size_t)(max_tiles + 1) * 2);
     t->tile_done = cv.take<u32>((max_tiles + 31) / 32);
+    t->tile_order = cv.take<u32>(max_tiles);
     t->state_c = cv.take<float4>((size_t)max_width * max_height);
     t->state_t = cv.take<float>((size_t)max_width * max_height);
     t->radix_control = cv.take<u32>(kRadixControlBytes / sizeof(u32));
-    t->pair_tile = cv.take<u32>(pairs);
+    t->pair_key = cv.take<u32>(pairs);
     t->pair_splat = cv.take<u32>(pairs);
-    t->pair_tile_alt = cv.take<u32>(pairs);
-    t->pair_splat_alt = cv.take<u32>(pairs);
     t->status_bytes_begin = cv.offset;
     t->cull_status = cv.take<u64>((n + kCullTile - 1) / kCullTile);
-    t->radix_status_words = radix_status_words(std::max(n, pairs));
+    t->radix_status_words = radix_status_words(n);
     t->radix_status = cv.take<u64>(t->radix_status_words);
     t->status_bytes_end = cv.offset;
   };
@@ -544,11 +542,8 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   // Depth slabs, nearest first (one slab when nothing is visible).
   const u32 slabs = n > 0 ? c->slab_count : 1;
   if (ev) c->frame_slabs[(c->timed_frames - 1) % gs_context::kTimingRing] = slabs;
-  u32 tile_bits = 0;
-  while (tile_bits < 32 && (1ull << tile_bits) < tiles) ++tile_bits;
   for (u32 k = 0; k < slabs; ++k) {
     const int e = 3 + 4 * (int)k;
-    GS_TRY(cudaMemsetAsync(c->tile_range, 0, (size_t)tiles * 2 * sizeof(u32), st));
     BinArgs ba{};
     ba.index = index;
     ba.visible_count = c->frame + FW_VISIBLE;
@@ -562,55 +557,25 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     ba.tiles_x = tiles_x;
     ba.tiles_y = tiles_y;
     ba.count = c->bin_count;
-    ba.block_sum = c->bin_block_sum;
+    ba.diff = c->bin_diff;
+    ba.tile_range = c->tile_range;
+    ba.tile_order = c->tile_order;
     ba.giant_list = c->giant_list;
     ba.giant_count = c->frame + FW_GIANTS + k;
-    ba.pair_tile = c->pair_tile;
+    ba.pair_key = c->pair_key;
     ba.pair_splat = c->pair_splat;
     ba.pair_capacity = c->pair_capacity;
-    ba.pair_count = c->frame + FW_PAIR_COUNT;
     ba.slab_pairs = c->frame + FW_SLAB_PAIRS;
     ba.pair_total = c->frame + FW_PAIR_TOTAL;
     ba.pair_sum = reinterpret_cast<unsigned long long*>(c->frame + FW_PAIR_SUM);
     ba.err = c->err;
-    GS_TRY(launch_bin(ba, st, nullptr, nullptr, c->num_sms));
-    GS_MARK(e);
-
-    // Stable sort of the slab's pairs by tile id alone: each tile's list keeps the draw order.
-    const u32* sorted_tile = c->pair_tile;
-    const u32* sorted_splat = c->pair_splat;
-    if (n > 0 && tile_bits > 0) {
-      RadixSortArgs ra{};
-      ra.keys = c->pair_tile;
-      ra.values = c->pair_splat;
-      ra.keys_alt = c->pair_tile_alt;
-      ra.values_alt = c->pair_splat_alt;
-      ra.count = c->frame + FW_PAIR_COUNT;
-      ra.max_count = c->pair_capacity;
-      ra.begin_bit = 0;
-      ra.end_bit = tile_bits;
-      ra.control = c->radix_control;
-      ra.status = c->radix_status;
-      const u32 passes = radix_passes(0, tile_bits);
-      ra.epoch = c->take_epochs(passes);
-      ra.err = c->err;
-      ra.num_sms = c->num_sms;
-      GS_TRY(radix_sort(ra, st));
-      if (passes & 1u) {
-        sorted_tile = c->pair_tile_alt;
-        sorted_splat = c->pair_splat_alt;
-      }
-    }
-    GS_MARK(e + 1);
-    if (n > 0)
-      GS_TRY(launch_tile_ranges(sorted_tile, c->frame + FW_PAIR_COUNT, c->pair_capacity, c->tile_range, c->num_sms,
-                                st));
+    GS_TRY(launch_bin(ba, st, ev ? ev[e] : nullptr, ev ? ev[e + 1] : nullptr, c->num_sms));
     GS_MARK(e + 2);
 
     RasterArgs rr{};
     rr.tile_range = c->tile_range;
     rr.pair_capacity = c->pair_capacity;
-    rr.pair_splat = sorted_splat;
+    rr.pair_splat = c->pair_splat;
     rr.record = c->record;
     rr.width = W;
     rr.height = H;

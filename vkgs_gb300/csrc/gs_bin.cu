@@ -1,37 +1,44 @@
-// gs_bin.cu -- (splat, tile) pairs in draw order, grouped by tile.
+// gs_bin.cu -- per-tile lists of (splat, tile) pairs in draw order.
 //
 // The reference draws one quad per sorted splat with the fixed-function rasteriser
 // (splat.vert:10-25, engine.cc:1474-1479); the blend order of every pixel is the sorted order.  Here
-// each 16x16 tile receives the list of splats whose 3-sigma quad can cover one of its pixel centres:
-//   1. count : per sorted splat, the number of tiles its quad reaches -> count[r]
-//   2. scan  : exclusive scan of count[] -> first[r] and the pair total P (reduce-then-scan, no waits)
-//   3. emit  : each warp lists the row spans of 32 consecutive sorted splats in shared memory and its
-//              lanes take consecutive pairs (span found by binary search), storing them coalesced at
-//              [first[r0], ...): pairs leave in ascending sorted position, and a splat covering
-//              thousands of tiles is spread over the whole warp
-//   4. a stable radix sort on the tile id alone (gs_sort.cu) then groups them by tile without
-//      disturbing that order, and tile ranges are read off the sorted tile ids.
-// Everything runs over one depth slab of the sorted splats at a time (sorted positions [lo, hi)); from
-// the second slab on, tiles that an earlier slab finished (tile_done bitmap) receive no pairs.
+// each 16x16 tile receives the list of splats whose 3-sigma quad can cover one of its pixel centres,
+// ascending in sorted position.  Everything runs over one depth slab of the sorted splats at a time
+// (sorted positions [lo, hi)); from the second slab on, tiles that an earlier slab finished
+// (tile_done bitmap) receive no pairs.  Per slab:
+//   1. count : per splat, its row spans (one tile row of the quad's footprint) enter a per-row
+//              difference array of tile counts (shared memory, then global atomics); splats whose
+//              footprint box spans more than kGiantPairs tiles are listed as giants and counted by
+//              one CTA each (k_bin_giant_count)
+//   2. scan  : one CTA turns the difference rows into tile counts and an exclusive scan over tiles:
+//              tile t owns pair slots [start_t, start_{t+1}), its cursor starts at start_t
+//   3. emit  : warps expand 32 sorted splats' pairs (span lists, giants by whole CTAs) and append the
+//              splat's sorted position to its tile's segment through the cursor (atomicAdd): each
+//              segment holds the right set of splats in arbitrary order
+//   4. sort  : one CTA per tile, longest segments first, sorts its segment by sorted position
+//              (comparison ranks for short segments, LSD radix in shared memory over the segment's
+//              key range otherwise) and writes the splat ids; a tile whose cursor did not end exactly
+//              at its segment end fails the self-check.
 // The tile test is exact up to a small margin: the quad (corners c +- a +- b) is clipped to each tile
 // row's band of pixel centres and the tile columns its x-extent reaches are taken; the margin only
 // ever adds pairs.  count and emit evaluate the same footprint arithmetic (this unit is compiled
-// without FMA contraction) and emit checks that every splat produced exactly its counted pairs.
+// without FMA contraction).
 #include "gs_common.cuh"
 #include "gs_internal.h"
 
 namespace gs {
 
-constexpr u32 kCountThreads = 256;
+constexpr u32 kCountThreads = 512;
+constexpr u32 kCountSmemWords = 12 * 1024;  // difference rows held in shared memory up to this size
 constexpr u32 kEmitThreads = 256;
 constexpr u32 kEmitWarps = kEmitThreads / 32;
-constexpr u32 kScanThreads = 256;
-constexpr u32 kScanItems = 16;
-constexpr u32 kScanTile = kScanThreads * kScanItems;  // counts per scan block
 constexpr float kMarginPx = 0.25f;
-constexpr u32 kGiantPairs = 128;    // splats with more pairs are expanded by a whole CTA (k_bin_giants)
+constexpr u32 kGiantPairs = 128;    // splats whose footprint box spans more tiles go to the CTA kernels
 constexpr u32 kGiantThreads = 256;
-constexpr u32 kGiantRows = 1024;    // row prefix held in shared memory per pass
+constexpr u32 kGiantRows = 1024;    // row prefix held in shared memory per window
+constexpr u32 kSortThreads = 256;
+constexpr u32 kSortWarps = kSortThreads / 32;
+constexpr u32 kSortChunk = 3072;    // keys ranked per shared-memory round
 
 // The quad of one splat prepared for row clipping: corners in order and inverse edge slopes.
 struct Footprint {
@@ -164,96 +171,183 @@ __device__ __forceinline__ SlabBounds slab(const BinArgs& a) {
   return slab_bounds(min(*a.visible_count, a.n), a.slab_e0, a.slab_e1);
 }
 
-// 1. pairs per sorted splat
+// Upper bound on the pairs of a footprint: its tile rows times the tile columns of its x-extent.
+__device__ __forceinline__ u32 footprint_box_pairs(const Footprint& f, const TargetGeom& g) {
+  if (f.ty1 < f.ty0) return 0;
+  const float xmin = fminf(fminf(f.vx[0], f.vx[1]), fminf(f.vx[2], f.vx[3]));
+  const float xmax = fmaxf(fmaxf(f.vx[0], f.vx[1]), fmaxf(f.vx[2], f.vx[3]));
+  const float mx = 2.0f * kMarginPx * g.inv_w;
+  int x0, x1;
+  pixel_range(xmin - mx, xmax + mx, g.width, x0, x1);
+  if (x1 < x0) return 0;
+  return (u32)(f.ty1 - f.ty0 + 1) * (u32)(x1 / (int)kTile - x0 / (int)kTile + 1);
+}
+
+// Adds the open tiles of row span [tx0, tx1] of tile row ty to the difference row (diff: the row's
+// tiles_x + 1 words); returns the number of open tiles.
+__device__ __forceinline__ u32 add_span(u32* diff, const u32* __restrict__ done, const TargetGeom& g, u32 ty,
+                                        u32 tx0, u32 tx1) {
+  const u32 base = ty * g.tiles_x;
+  const u32 nd = done ? done_in_range(done, base + tx0, base + tx1) : 0u;
+  const u32 width = tx1 - tx0 + 1;
+  if (nd == 0) {
+    atomicAdd(diff + tx0, 1u);
+    atomicAdd(diff + tx1 + 1, 0xffffffffu);
+  } else if (nd < width) {  // the span straddles finished tiles: add its open tiles one by one
+    for (u32 tx = tx0; tx <= tx1; ++tx) {
+      if (tile_is_done(done, base + tx)) continue;
+      atomicAdd(diff + tx, 1u);
+      atomicAdd(diff + tx + 1, 0xffffffffu);
+    }
+  }
+  return width - nd;
+}
+
+// 1. per-tile pair counts (difference rows) and per-splat open pair counts; giants listed
+template <bool SMEM>
 __global__ __launch_bounds__(kCountThreads) void k_bin_count(const BinArgs a) {
+  extern __shared__ u32 s_diff[];
+  const u32 rw = a.tiles_x + 1, dw = a.tiles_y * rw;
+  u32* diff = SMEM ? s_diff : a.diff;
+  if (SMEM) {
+    for (u32 i = threadIdx.x; i < dw; i += blockDim.x) s_diff[i] = 0;
+    __syncthreads();
+  }
   const SlabBounds sb = slab(a);
   const TargetGeom g = target_geom(a);
   const u32 stride = gridDim.x * blockDim.x;
   for (u32 r = sb.lo + blockIdx.x * blockDim.x + threadIdx.x; r < sb.hi; r += stride) {
     Footprint f;
     u32 c = 0;
-    if (footprint(a.record, __ldg(a.index + r), g, f))
-      c = a.tile_done ? footprint_open_pairs(f, g, a.tile_done) : footprint_pairs(f, g);
-    a.count[r] = c;
-    if (c > kGiantPairs) a.giant_list[atomicAdd(a.giant_count, 1u)] = r;
+    if (footprint(a.record, __ldg(a.index + r), g, f)) {
+      if (footprint_box_pairs(f, g) > kGiantPairs) {
+        a.giant_list[atomicAdd(a.giant_count, 1u)] = r;
+      } else {
+        for (int ty = f.ty0; ty <= f.ty1; ++ty) {
+          int tx0, tx1;
+          footprint_cols(f, g, ty, tx0, tx1);
+          if (tx1 >= tx0) c += add_span(diff + (u32)ty * rw, a.tile_done, g, (u32)ty, (u32)tx0, (u32)tx1);
+        }
+      }
+    }
+    a.count[r] = c;  // 0 for giants: k_bin_giant_emit writes theirs
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (u32 i = threadIdx.x; i < dw; i += blockDim.x) {
+      const u32 v = s_diff[i];
+      if (v) atomicAdd(a.diff + i, v);
+    }
   }
 }
 
-// 2a. per-block sums of count[]
-__global__ __launch_bounds__(kScanThreads) void k_bin_reduce(const BinArgs a) {
-  __shared__ u32 s_scan[32];
-  const SlabBounds sb = slab(a);
-  const u32 base = sb.lo + blockIdx.x * kScanTile;
-  if (base >= sb.hi) return;
-  u32 s = 0;
-#pragma unroll
-  for (u32 i = 0; i < kScanItems; ++i) {
-    const u32 r = base + i * kScanThreads + threadIdx.x;
-    s += r < sb.hi ? a.count[r] : 0u;
+// Row spans of one giant's footprint rows [w0, w0 + m): s_base[i] = first tile id of row i, s_pfx =
+// exclusive prefix of the widths, s_pfx[m] = total.  Whole CTA.
+__device__ __forceinline__ u32 giant_rows(const Footprint& f, const TargetGeom& g, u32 w0, u32 m, u32* s_pfx,
+                                          u32* s_base, u32* s_scan) {
+  u32 carry = 0;
+  for (u32 i0 = 0; i0 < m; i0 += kGiantThreads) {
+    const u32 i = i0 + threadIdx.x;
+    u32 width = 0;
+    if (i < m) {
+      const int ty = f.ty0 + (int)(w0 + i);
+      int tx0, tx1;
+      footprint_cols(f, g, ty, tx0, tx1);
+      width = (u32)max(0, tx1 - tx0 + 1);
+      s_base[i] = (u32)ty * g.tiles_x + (u32)max(tx0, 0);
+    }
+    u32 tot;
+    const u32 ex = block_exclusive_scan<kGiantThreads>(width, s_scan, &tot);
+    if (i < m) s_pfx[i] = carry + ex;
+    carry += tot;
   }
-  u32 total;
-  block_exclusive_scan<kScanThreads>(s, s_scan, &total);
-  if (threadIdx.x == 0) a.block_sum[blockIdx.x] = total;
-}
-
-// 2b. exclusive scan of the block sums (one CTA), the pair total and the capacity check
-__global__ __launch_bounds__(1024) void k_bin_scan_blocks(const BinArgs a) {
-  __shared__ u32 s_scan[32];
-  __shared__ u32 s_carry;
-  const SlabBounds sb = slab(a);
-  const u32 nblocks = (sb.hi - sb.lo + kScanTile - 1) / kScanTile;
-  if (threadIdx.x == 0) s_carry = 0;
+  if (threadIdx.x == 0) s_pfx[m] = carry;
   __syncthreads();
-  for (u32 b0 = 0; b0 < nblocks; b0 += 1024) {
-    const u32 b = b0 + threadIdx.x;
-    const u32 x = b < nblocks ? a.block_sum[b] : 0u;
-    u32 sum;
-    const u32 excl = block_exclusive_scan<1024>(x, s_scan, &sum);
-    if (b < nblocks) a.block_sum[b] = s_carry + excl;
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += sum;
-    __syncthreads();
+  return carry;
+}
+
+// 1b. giants' tile counts: one CTA per giant, one thread per tile row
+__global__ __launch_bounds__(kGiantThreads) void k_bin_giant_count(const BinArgs a) {
+  const u32 ng = *a.giant_count;
+  const TargetGeom g = target_geom(a);
+  const u32 rw = a.tiles_x + 1;
+  for (u32 k = blockIdx.x; k < ng; k += gridDim.x) {
+    Footprint f;
+    footprint(a.record, __ldg(a.index + a.giant_list[k]), g, f);
+    for (int ty = f.ty0 + (int)threadIdx.x; ty <= f.ty1; ty += kGiantThreads) {
+      int tx0, tx1;
+      footprint_cols(f, g, ty, tx0, tx1);
+      if (tx1 >= tx0) add_span(a.diff + (u32)ty * rw, a.tile_done, g, (u32)ty, (u32)tx0, (u32)tx1);
+    }
+  }
+}
+
+// 2. tile counts -> segments.  One CTA: warps turn difference rows into counts (and clear them),
+//    then an exclusive scan over the tiles in row-major order sets each tile's start and cursor.
+__global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_len[33];
+  const u32 tiles_x = a.tiles_x, rw = tiles_x + 1, T = tiles_x * a.tiles_y;
+  const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  for (u32 row = warp; row < a.tiles_y; row += 32) {
+    u32 carry = 0;
+    for (u32 c0 = 0; c0 < rw; c0 += 32) {
+      const u32 c = c0 + lane;
+      u32 v = 0;
+      if (c < rw) {
+        v = a.diff[row * rw + c];
+        a.diff[row * rw + c] = 0;
+      }
+      u32 incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (u32)o) incl += y;
+      }
+      if (c < tiles_x) a.tile_range[2 * (row * tiles_x + c) + 1] = carry + incl;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+  }
+  __syncthreads();
+  const u32 per = (T + 1023) / 1024;
+  const u32 b = min(threadIdx.x * per, T), e = min(b + per, T);
+  u32 s = 0;
+  for (u32 t = b; t < e; ++t) s += a.tile_range[2 * t + 1];
+  u32 total;
+  u32 run = block_exclusive_scan<1024>(s, s_scan, &total);
+  if (threadIdx.x < 33) s_len[threadIdx.x] = 0;
+  __syncthreads();
+  for (u32 t = b; t < e; ++t) {
+    const u32 c = a.tile_range[2 * t + 1];
+    a.tile_range[2 * t] = run;
+    a.tile_range[2 * t + 1] = run;
+    run += c;
+    atomicAdd(&s_len[32 - __clz(c)], 1u);
   }
   if (threadIdx.x == 0) {
-    const u32 P = s_carry;
-    *a.slab_pairs = P;
-    *a.pair_count = min(P, a.pair_capacity);
-    atomicMax(a.pair_total, P);
-    *a.pair_sum += P;
-    if (P > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
-  }
-}
-
-// 2c. count[] -> exclusive prefix (first pair of each splat), in place
-__global__ __launch_bounds__(kScanThreads) void k_bin_scan(const BinArgs a) {
-  __shared__ u32 s_scan[32];
-  __shared__ u32 s_vals[kScanTile];
-  const SlabBounds sb = slab(a);
-  const u32 base = sb.lo + blockIdx.x * kScanTile;
-  if (base >= sb.hi) return;
-  // blocked arrangement: thread t owns elements [t*items, (t+1)*items) of the block
-  for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
-    const u32 r = base + i;
-    s_vals[i] = r < sb.hi ? a.count[r] : 0u;
+    a.tile_range[2 * T] = total;  // sentinel: end of the last segment
+    a.tile_range[2 * T + 1] = total;
   }
   __syncthreads();
-  u32 x[kScanItems], s = 0;
-#pragma unroll
-  for (u32 i = 0; i < kScanItems; ++i) {
-    x[i] = s_vals[threadIdx.x * kScanItems + i];
-    s += x[i];
-  }
-  u32 total;
-  u32 run = a.block_sum[blockIdx.x] + block_exclusive_scan<kScanThreads>(s, s_scan, &total);
-#pragma unroll
-  for (u32 i = 0; i < kScanItems; ++i) {
-    s_vals[threadIdx.x * kScanItems + i] = run;
-    run += x[i];
+  // processing order of the per-tile sort: longest segments first (buckets by bit length)
+  if (threadIdx.x == 0) {
+    u32 acc = 0;
+    for (int k = 32; k >= 0; --k) {
+      const u32 c = s_len[k];
+      s_len[k] = acc;
+      acc += c;
+    }
   }
   __syncthreads();
-  for (u32 i = threadIdx.x; i < kScanTile; i += kScanThreads) {
-    const u32 r = base + i;
-    if (r < sb.hi) a.count[r] = s_vals[i];
+  for (u32 t = b; t < e; ++t) {
+    const u32 c = a.tile_range[2 * t + 2] - a.tile_range[2 * t];
+    a.tile_order[atomicAdd(&s_len[32 - __clz(c)], 1u)] = t;
+  }
+  if (threadIdx.x == 0) {
+    *a.slab_pairs = total;
+    atomicMax(a.pair_total, total);
+    *a.pair_sum += total;
+    if (total > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
   }
 }
 
@@ -342,177 +436,234 @@ __device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const 
   return done;
 }
 
-// 3. emission: warp w walks 32 consecutive sorted splats' pairs -- splat by splat, row-major inside a
-//    splat -- with the span list of for_each_pair, drops pairs of finished tiles, and stores the rest
-//    coalesced into the group's contiguous output range [first[r0], ...): pairs leave in ascending
-//    sorted position.
+// 3. emission: warp w walks the pairs of 32 consecutive sorted splats with the span list of
+//    for_each_pair and appends each open pair's sorted position to its tile's segment.
 __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
   __shared__ u32 s_spans[kEmitWarps][2 * (kSpanBuf + 1)];
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const SlabBounds sb = slab(a);
-  const u32 P = *a.slab_pairs;
   const TargetGeom g = target_geom(a);
   const u32 gwarps = gridDim.x * kEmitWarps;
-  const u32 lt = lanemask_lt();
   for (u32 r0 = sb.lo + (blockIdx.x * kEmitWarps + warp) * 32; r0 < sb.hi; r0 += gwarps * 32) {
-    const u32 gfirst = a.count[r0];  // exclusive prefix after the scan
-    const u32 rl = min(r0 + 32u, sb.hi);
-    const u32 gend = rl < sb.hi ? a.count[rl] : P;
-    if (gfirst == gend) continue;  // no open pair in this group (warp-uniform)
     const u32 r = r0 + lane;
+    const u32 c = r < sb.hi ? a.count[r] : 0u;
+    if (__ballot_sync(0xffffffffu, c > 0) == 0) continue;  // nothing open in this group
     Footprint f;
     bool ok = false;
-    u32 id = 0, giant = 0;
-    if (r < sb.hi) {
-      const u32 mine = (r + 1 < sb.hi ? a.count[r + 1] : P) - a.count[r];
-      if (mine > kGiantPairs) {
-        giant = mine;  // k_bin_giants writes these
-      } else {
-        id = __ldg(a.index + r);
-        ok = footprint(a.record, id, g, f);
-      }
-    }
-    // giant pairs of the lanes before this one: the gaps their ranges leave in the group's output
-    u32 gincl = giant;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const u32 y = __shfl_up_sync(0xffffffffu, gincl, o);
-      if (lane >= (u32)o) gincl += y;
-    }
-    const u32 gexcl = gincl - giant, gtotal = __shfl_sync(0xffffffffu, gincl, 31);
-    u32 kept = 0;  // pairs of non-giant splats written so far
+    if (c > 0) ok = footprint(a.record, __ldg(a.index + r), g, f);
     for_each_pair(f, ok, g, s_spans[warp], [&](bool has, u32 tile, u32 owner, u32) {
-      const u32 oid = __shfl_sync(0xffffffffu, id, owner);
-      const u32 gap = __shfl_sync(0xffffffffu, gexcl, owner);
-      const bool keep = has && !(a.tile_done && tile_is_done(a.tile_done, tile));
-      const u32 ballot = __ballot_sync(0xffffffffu, keep);
-      const u32 pos = gfirst + gap + kept + __popc(ballot & lt);
-      if (keep && pos < a.pair_capacity) {
-        a.pair_tile[pos] = tile;
-        a.pair_splat[pos] = oid;
+      if (has && !(a.tile_done && tile_is_done(a.tile_done, tile))) {
+        const u32 pos = atomicAdd(a.tile_range + 2 * tile + 1, 1u);
+        if (pos < a.pair_capacity) a.pair_key[pos] = r0 + owner;
       }
-      kept += __popc(ballot);
     });
-    if (lane == 0 && gfirst + gtotal + kept != gend) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
   }
 }
 
-// 3b. giants: one CTA per splat with more than kGiantPairs pairs.  Its rows' spans are listed in
-//     shared memory with a block-wide prefix, every thread takes pairs j = tid, tid + 256, ... and
-//     finds its row by binary search, and open pairs are packed into the splat's output range (the
-//     order inside one splat's range is free: a splat meets each tile once, and the stable tile sort
-//     only orders pairs of different splats).
-__global__ __launch_bounds__(kGiantThreads) void k_bin_giants(const BinArgs a) {
+// 3b. giants: one CTA per listed splat; every thread takes pairs j = tid, tid + 256, ... of the row
+//     span list and finds its row by binary search.
+__global__ __launch_bounds__(kGiantThreads) void k_bin_giant_emit(const BinArgs a) {
   __shared__ u32 s_pfx[kGiantRows + 1];
   __shared__ u32 s_base[kGiantRows];
   __shared__ u32 s_scan[32];
-  __shared__ u32 s_cursor;
-  const SlabBounds sb = slab(a);
-  const u32 P = *a.slab_pairs;
   const u32 ng = *a.giant_count;
   const TargetGeom g = target_geom(a);
-  const u32 tid = threadIdx.x, lane = tid & 31u;
   for (u32 k = blockIdx.x; k < ng; k += gridDim.x) {
     const u32 r = a.giant_list[k];
-    const u32 first = a.count[r];
-    const u32 end = r + 1 < sb.hi ? a.count[r + 1] : P;
     Footprint f;
-    const u32 id = __ldg(a.index + r);
-    footprint(a.record, id, g, f);
-    if (tid == 0) s_cursor = 0;
+    footprint(a.record, __ldg(a.index + r), g, f);
     const u32 nrows = (u32)max(0, f.ty1 - f.ty0 + 1);
     for (u32 w0 = 0; w0 < nrows; w0 += kGiantRows) {  // windows of rows (one for any real target)
       const u32 m = min(kGiantRows, nrows - w0);
-      u32 carry = 0;
-      for (u32 i0 = 0; i0 < m; i0 += kGiantThreads) {
-        const u32 i = i0 + tid;
-        u32 width = 0;
-        if (i < m) {
-          const int ty = f.ty0 + (int)(w0 + i);
-          int tx0, tx1;
-          footprint_cols(f, g, ty, tx0, tx1);
-          width = (u32)max(0, tx1 - tx0 + 1);
-          s_base[i] = (u32)ty * g.tiles_x + (u32)max(tx0, 0);
+      const u32 total = giant_rows(f, g, w0, m, s_pfx, s_base, s_scan);
+      for (u32 j = threadIdx.x; j < total; j += kGiantThreads) {
+        u32 lo = 0, hi = m;  // last row with s_pfx[row] <= j
+        while (hi - lo > 1) {
+          const u32 mid = (lo + hi) >> 1;
+          if (s_pfx[mid] <= j) lo = mid;
+          else hi = mid;
         }
-        u32 tot;
-        const u32 ex = block_exclusive_scan<kGiantThreads>(width, s_scan, &tot);
-        if (i < m) s_pfx[i] = carry + ex;
-        carry += tot;
-        __syncthreads();
-      }
-      if (tid == 0) s_pfx[m] = carry;
-      __syncthreads();
-      for (u32 j0 = 0; j0 < carry; j0 += kGiantThreads) {
-        const u32 j = j0 + tid;
-        bool keep = false;
-        u32 tile = 0;
-        if (j < carry) {
-          u32 lo = 0, hi = m;  // last row with s_pfx[row] <= j
-          while (hi - lo > 1) {
-            const u32 mid = (lo + hi) >> 1;
-            if (s_pfx[mid] <= j) lo = mid;
-            else hi = mid;
-          }
-          tile = s_base[lo] + (j - s_pfx[lo]);
-          keep = !(a.tile_done && tile_is_done(a.tile_done, tile));
-        }
-        const u32 ballot = __ballot_sync(0xffffffffu, keep);
-        u32 wbase = 0;
-        if (lane == 0 && ballot) wbase = atomicAdd(&s_cursor, (u32)__popc(ballot));
-        wbase = __shfl_sync(0xffffffffu, wbase, 0);
-        const u32 pos = first + wbase + __popc(ballot & lanemask_lt());
-        if (keep && pos < end && pos < a.pair_capacity) {
-          a.pair_tile[pos] = tile;
-          a.pair_splat[pos] = id;
-        }
+        const u32 tile = s_base[lo] + (j - s_pfx[lo]);
+        if (a.tile_done && tile_is_done(a.tile_done, tile)) continue;
+        const u32 pos = atomicAdd(a.tile_range + 2 * tile + 1, 1u);
+        if (pos < a.pair_capacity) a.pair_key[pos] = r;
       }
       __syncthreads();
     }
-    if (tid == 0 && s_cursor != end - first) atomicOr(a.err, ERR_INTERNAL);  // count and emit disagree
+  }
+}
+
+// Stable ranking of keys[0..cnt) (shared memory) on digit ((key - kmin) >> shift) & 0xff.  Warp w owns
+// elements [w * 32 * ipw, (w + 1) * 32 * ipw), item i of a lane is element w * 32 * ipw + i * 32 + lane.
+// Leaves s_rank[e] = rank among the warp's earlier elements of the same digit, s_whist[w][d] = the
+// elements of digit d in warps before w, s_dcount[d] = the digit's total.  Whole CTA.
+__device__ __forceinline__ void rank_chunk(const u32* keys, u32 cnt, u32 shift, u32 kmin, unsigned short* s_rank,
+                                           u32 (*s_whist)[256], u32* s_dcount) {
+  const u32 tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  for (u32 i = tid; i < kSortWarps * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+  __syncthreads();
+  const u32 ipw = (cnt + kSortThreads - 1) / kSortThreads;
+  const u32 wbase = warp * 32 * ipw;
+  const u32 lt = lanemask_lt();
+  for (u32 i = 0; i < ipw; ++i) {
+    const u32 e = wbase + i * 32 + lane;
+    const bool valid = e < cnt;
+    const u32 d = valid ? ((keys[e] - kmin) >> shift) & 0xffu : 0u;
+    const u32 peers = match_digit8(d, valid);
+    const int leader = valid ? __ffs(peers) - 1 : 0;
+    u32 old = 0;
+    if (valid && (int)lane == leader) old = atomicAdd(&s_whist[warp][d], (u32)__popc(peers));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    if (valid) s_rank[e] = (unsigned short)(old + __popc(peers & lt));
+  }
+  __syncthreads();
+  u32 acc = 0;
+#pragma unroll
+  for (u32 w = 0; w < kSortWarps; ++w) {
+    const u32 c = s_whist[w][tid];
+    s_whist[w][tid] = acc;
+    acc += c;
+  }
+  s_dcount[tid] = acc;
+  __syncthreads();
+}
+
+// 4. one CTA per tile (longest segments first): sort the segment's sorted positions ascending and
+//    write the splat ids in that order.  Up to kSortThreads keys: rank by comparison; up to
+//    kSortChunk: LSD radix in shared memory over the segment's key range; longer: the same passes
+//    streaming the segment through shared memory in chunks.
+__global__ __launch_bounds__(kSortThreads) void k_tile_sort(const BinArgs a) {
+  __shared__ u32 s_keys[2][kSortChunk];
+  __shared__ unsigned short s_rank[kSortChunk];
+  __shared__ u32 s_whist[kSortWarps][256];
+  __shared__ u32 s_dcount[256];
+  __shared__ u32 s_dpos[256];
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_red[2][kSortWarps];
+  const u32 t = a.tile_order[blockIdx.x], tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  if (a.tile_done && tile_is_done(a.tile_done, t)) return;
+  const u32 start = a.tile_range[2 * t], cursor = a.tile_range[2 * t + 1], end = a.tile_range[2 * t + 2];
+  if (tid == 0 && cursor != end) atomicOr(a.err, ERR_INTERNAL);  // emitted pairs != counted pairs
+  const u32 x = min(start, a.pair_capacity), n = min(cursor, a.pair_capacity) - x;
+  if (n == 0) return;
+  u32* key = a.pair_key + x;
+  u32* out = a.pair_splat + x;
+  if (n <= kSortThreads) {  // a key's rank by direct comparison with all the others (keys are distinct)
+    const u32 k = tid < n ? key[tid] : 0u;
+    s_keys[0][tid] = k;
     __syncthreads();
+    if (tid < n) {
+      u32 rank = 0;
+      for (u32 j = 0; j < n; ++j) rank += s_keys[0][j] < k ? 1u : 0u;
+      out[rank] = __ldg(a.index + k);
+    }
+    return;
   }
+  // key range of the segment: the radix passes cover only its bits
+  u32 kmin = 0xffffffffu, kmax = 0;
+  for (u32 e = tid; e < n; e += kSortThreads) {
+    const u32 k = key[e];
+    kmin = min(kmin, k);
+    kmax = max(kmax, k);
+    if (n <= kSortChunk) s_keys[0][e] = k;
+  }
+  kmin = __reduce_min_sync(0xffffffffu, kmin);
+  kmax = __reduce_max_sync(0xffffffffu, kmax);
+  if (lane == 0) {
+    s_red[0][warp] = kmin;
+    s_red[1][warp] = kmax;
+  }
+  __syncthreads();
+  kmin = s_red[0][0];
+  kmax = s_red[1][0];
+#pragma unroll
+  for (u32 w = 1; w < kSortWarps; ++w) {
+    kmin = min(kmin, s_red[0][w]);
+    kmax = max(kmax, s_red[1][w]);
+  }
+  const u32 bits = 32 - __clz(kmax - kmin);
+  const u32 passes = (bits + 7) / 8;
+  if (n <= kSortChunk) {  // the whole segment stays in shared memory
+    const u32 ipw = (n + kSortThreads - 1) / kSortThreads;
+    u32 cur = 0;
+    for (u32 p = 0; p < passes; ++p) {
+      const u32 shift = 8 * p;
+      rank_chunk(s_keys[cur], n, shift, kmin, s_rank, s_whist, s_dcount);
+      u32 tot;
+      s_dpos[tid] = block_exclusive_scan<kSortThreads>(s_dcount[tid], s_scan, &tot);
+      __syncthreads();
+      for (u32 i = 0; i < ipw; ++i) {
+        const u32 e = warp * 32 * ipw + i * 32 + lane;
+        if (e < n) {
+          const u32 k = s_keys[cur][e];
+          const u32 d = ((k - kmin) >> shift) & 0xffu;
+          s_keys[cur ^ 1][s_dpos[d] + s_whist[warp][d] + s_rank[e]] = k;
+        }
+      }
+      __syncthreads();
+      cur ^= 1;
+    }
+    for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + s_keys[cur][e]);
+    return;
+  }
+  // Longer segments: each pass streams the segment through shared memory in chunks, in order, with
+  // running digit offsets; the passes alternate between the key and the output array.
+  u32* src = key;
+  u32* dst = out;
+  for (u32 p = 0; p < passes; ++p) {
+    const u32 shift = 8 * p;
+    s_dcount[tid] = 0;
+    __syncthreads();
+    for (u32 e = tid; e < n; e += kSortThreads) atomicAdd(&s_dcount[((src[e] - kmin) >> shift) & 0xffu], 1u);
+    __syncthreads();
+    u32 tot;
+    s_dpos[tid] = block_exclusive_scan<kSortThreads>(s_dcount[tid], s_scan, &tot);
+    __syncthreads();
+    for (u32 base = 0; base < n; base += kSortChunk) {
+      const u32 cnt = min(kSortChunk, n - base);
+      for (u32 e = tid; e < cnt; e += kSortThreads) s_keys[0][e] = src[base + e];
+      __syncthreads();
+      rank_chunk(s_keys[0], cnt, shift, kmin, s_rank, s_whist, s_dcount);
+      const u32 cw = (cnt + kSortThreads - 1) / kSortThreads;
+      for (u32 i = 0; i < cw; ++i) {
+        const u32 e = warp * 32 * cw + i * 32 + lane;
+        if (e < cnt) {
+          const u32 k = s_keys[0][e];
+          const u32 d = ((k - kmin) >> shift) & 0xffu;
+          dst[s_dpos[d] + s_whist[warp][d] + s_rank[e]] = k;
+        }
+      }
+      __syncthreads();
+      s_dpos[tid] += s_dcount[tid];
+      __syncthreads();
+    }
+    u32* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + src[e]);  // in place when src == out
 }
 
-// 4. tile ranges from the tile-sorted pair keys
-__global__ void k_tile_ranges(const u32* __restrict__ tile, const u32* __restrict__ pair_count, u32 capacity,
-                              uint2* __restrict__ range) {
-  const u32 P = min(*pair_count, capacity);
-  const u32 stride = gridDim.x * blockDim.x;
-  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
-    const u32 t = tile[i];
-    if (i == 0 || tile[i - 1] != t) range[t].x = i;
-    if (i == P - 1 || tile[i + 1] != t) range[t].y = i + 1;
-  }
-}
+size_t bin_diff_words(u32 max_tiles_x, u32 max_tiles_y) { return (size_t)(max_tiles_x + 1) * max_tiles_y; }
 
-size_t bin_block_sums(u32 max_splats) { return (max(max_splats, 1u) + kScanTile - 1) / kScanTile; }
-
-cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_count, cudaEvent_t after_scan,
+cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_scan, cudaEvent_t after_emit,
                        int num_sms) {
-  if (a.n == 0) {
-    if (after_count) cudaEventRecord(after_count, stream);
-    if (after_scan) cudaEventRecord(after_scan, stream);
-    return cudaSuccess;
-  }
   const u32 sms = (u32)max(num_sms, 1);
-  const u32 count_grid = min((a.n + kCountThreads - 1) / kCountThreads, sms * 16u);
-  k_bin_count<<<count_grid, kCountThreads, 0, stream>>>(a);
-  if (after_count) cudaEventRecord(after_count, stream);
-  const u32 blocks = (u32)bin_block_sums(a.n);
-  k_bin_reduce<<<blocks, kScanThreads, 0, stream>>>(a);
-  k_bin_scan_blocks<<<1, 1024, 0, stream>>>(a);
-  k_bin_scan<<<blocks, kScanThreads, 0, stream>>>(a);
+  const u32 tiles = a.tiles_x * a.tiles_y;
+  const u32 dw = (a.tiles_x + 1) * a.tiles_y;
+  const u32 count_grid = max(1u, min((a.n + kCountThreads - 1) / kCountThreads, sms * 2u));
+  if (dw <= kCountSmemWords)
+    k_bin_count<true><<<count_grid, kCountThreads, dw * sizeof(u32), stream>>>(a);
+  else
+    k_bin_count<false><<<count_grid, kCountThreads, 0, stream>>>(a);
+  k_bin_giant_count<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
+  k_bin_scan<<<1, 1024, 0, stream>>>(a);
   if (after_scan) cudaEventRecord(after_scan, stream);
-  const u32 emit_grid = min((a.n + kEmitThreads - 1) / kEmitThreads, sms * 8u);
+  const u32 emit_grid = max(1u, min((a.n + kEmitThreads - 1) / kEmitThreads, sms * 8u));
   k_bin_emit<<<emit_grid, kEmitThreads, 0, stream>>>(a);
-  k_bin_giants<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_tile_ranges(const u32* pair_tile, const u32* pair_count, u32 capacity, u32* tile_range,
-                               int num_sms, cudaStream_t stream) {
-  const u32 grid = max(1u, min((capacity + 255) / 256, (u32)max(num_sms, 1) * 8u));
-  k_tile_ranges<<<grid, 256, 0, stream>>>(pair_tile, pair_count, capacity, reinterpret_cast<uint2*>(tile_range));
+  k_bin_giant_emit<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
+  if (after_emit) cudaEventRecord(after_emit, stream);
+  k_tile_sort<<<max(tiles, 1u), kSortThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

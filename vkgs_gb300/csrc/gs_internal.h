@@ -84,26 +84,25 @@ struct BinArgs {
   u32 slab_e0, slab_e1;      // this slab's share of V (slab_bounds)
   const u32* tile_done;      // bitmap of finished tiles (they get no pairs), or null
   u32 width, height, tiles_x, tiles_y;
-  u32* count;                // [n] pairs per sorted splat, then its first pair (exclusive prefix)
-  u32* block_sum;            // [bin_block_sums(n)]
-  u32* pair_tile;            // out: tile id per pair, pairs in sorted-splat order
-  u32* pair_splat;           // out: splat id per pair
+  u32* count;                // [n] open pairs per sorted splat (0 for giants)
+  u32* diff;                 // [bin_diff_words] per-row difference counts, all zero between slabs
+  u32* tile_range;           // [tiles + 1][2]: (segment start, cursor); the cursor ends at the next start
+  u32* tile_order;           // [tiles] tiles by descending segment length (the per-tile sort's order)
+  u32* giant_list;           // [n] sorted positions of splats with a footprint box above kGiantPairs
+  u32* giant_count;          // this slab's entries in giant_list (zeroed before the frame)
+  u32* pair_key;             // [capacity] sorted position per pair, grouped by tile
+  u32* pair_splat;           // [capacity] splat id per pair, grouped by tile, ascending sorted position
   u32 pair_capacity;
-  u32* giant_list;           // [n] sorted positions of splats with more than kGiantPairs pairs
-  u32* giant_count;          // this slab's entries in giant_list (zeroed before the slab)
-  u32* pair_count;           // out: min(slab pairs, capacity)
   u32* slab_pairs;           // out: pairs this slab needs
   u32* pair_total;           // out: max over the frame's slabs (atomicMax)
   unsigned long long* pair_sum;  // out: sum over the frame's slabs
   u32* err;
 };
 
-size_t bin_block_sums(u32 max_splats);
-// Records after_count / after_scan (when non-null) between the count, scan and emit steps.
-cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_count, cudaEvent_t after_scan,
+size_t bin_diff_words(u32 max_tiles_x, u32 max_tiles_y);
+// count + scan, event after_scan, emit, event after_emit, per-tile sort (events may be null).
+cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_scan, cudaEvent_t after_emit,
                        int num_sms);
-cudaError_t launch_tile_ranges(const u32* pair_tile, const u32* pair_count, u32 capacity, u32* tile_range /*2*T*/,
-                               int num_sms, cudaStream_t stream);
 
 // ---- raster (gs_raster.cu) ----
 struct RasterArgs {
