@@ -36,6 +36,7 @@ METRIC = "frames/s at 6M splats 1600x900"
 UNIT = "frames/s"
 OPS_PER_FRAGMENT = 20  # FP32 lane-ops per covered (pixel, splat) pair, the blend's algorithmic cost
 WORKLOAD = "large"
+DEFAULT_SLABS = 2  # the renderer's default depth-slab schedule: nearest 1/8 of the visible splats, then the rest
 
 
 def parse_args():
@@ -261,6 +262,12 @@ def run_ours(args):
     ms_max = float(t.item())
     value = world * K / (ms_max / 1000.0)
 
+    # (splat, tile) pairs binned per camera on the timed path (depth slabs, finished tiles skipped)
+    emitted = []
+    for cam in cams:
+        r.render(splats, cam, color=color)
+        emitted.append(r.check()["pairs_emitted"])
+
     # End to end through the public API: per step the camera crosses into the kernel parameters
     # (h2d) and the finished RGBA image is copied into pinned host memory (d2h).
     host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
@@ -329,7 +336,8 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{WORKLOAD}: {n} splats (70% shell r=4, 30% uniform), 1600x900, 9 cameras "
                                "(8 on an r=8 circle + 1 at r=20), SH degree 3 in binary16",
-                   "parallelism": f"replicas x{world}", "l2": "inputs (816 MB) exceed L2; no flush"},
+                   "parallelism": f"replicas x{world}", "l2": "inputs (816 MB) exceed L2; no flush",
+                   "depth_slabs": "nearest 128/1024 of the visible splats, then the rest"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 292, "d2h_bytes_per_step": H * W * 16},
         "gpu_launches": None,
         "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
@@ -342,13 +350,14 @@ def run_ours(args):
         "dominant_stage": dominant,
         "frame_stats": {"visible": [s["visible_count"] for s in stats], "tile_pairs": [s["tile_pairs"] for s in stats],
                         "fragments": [s["fragments"] for s in stats],
-                        "fragments_blended": [s["fragments_blended"] for s in stats]},
+                        "fragments_blended": [s["fragments_blended"] for s in stats],
+                        "pairs_emitted": emitted},
         "cpu_baseline": cpu,
         "clocks": clk,
     }
-    # cull_project, depth sort (histogram + 4 passes), binning (count, reduce, block scan, scan, emit),
-    # tile sort (histogram + 2 passes), tile ranges, raster
-    launches_per_frame = 1 + 5 + 5 + 3 + 1 + 1
+    # cull_project, depth sort (histogram + 4 passes), then per depth slab: count, giant count, scan,
+    # emit, giant emit, per-tile sort, raster
+    launches_per_frame = 1 + 5 + 7 * DEFAULT_SLABS
     line["gpu_launches"] = launches_per_frame * K
     print(json.dumps(line), flush=True)
     if dist is not None:
