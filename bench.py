@@ -48,6 +48,7 @@ def parse_args():
     p.add_argument("--splats", type=int, default=None, help="override the splat count (testing only)")
     p.add_argument("--cpu-band-stride", type=int, default=8, help="CPU sample: blend every k-th 16-row band")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-forms", action="store_true", help="skip the batched / differentiation forms")
     return p.parse_args()
 
 
@@ -159,6 +160,66 @@ def cpu_frames(oracle, act, cams, band_stride: int, steps: int, threads: int):
         t2 = time.perf_counter()
         out.append((t1 - t0) + band_stride * (t2 - t1))
     return out
+
+
+def batched_form(dev, quick: bool = False):
+    """Batched views (1M splats, 64 random cameras of mixed resolution): one gs_render_batched call captured
+    in a CUDA graph and replayed, against the plain per-view loop of gs_render calls on the same GPU."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer, parse_ply, synthetic as syn
+    from vkgs_gb300.autotune import autotune_batched
+
+    rows, off, specs = syn.workload("batched")
+    splats = parse_ply(torch.from_numpy(rows).to(dev), off)
+    del rows
+    cams = [Camera.from_spec(sp) for sp in specs]
+    colors = [torch.empty((c.height, c.width, 4), dtype=torch.float32, device=dev) for c in cams]
+    r = Renderer(splats.count, 1920, 1080)
+    for cam, col in zip(cams, colors):
+        r.render_checked(splats, cam, color=col)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 2 if quick else 5
+
+    def loop():
+        for cam, col in zip(cams, colors):
+            r.render(splats, cam, color=col)
+
+    loop()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        loop()
+    e1.record()
+    torch.cuda.synchronize()
+    loop_ms = e0.elapsed_time(e1) / reps
+    r.check()
+    choice = autotune_batched(r, splats, cams, colors, reps=2 if quick else 4)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        r.render_batched(splats, cams, colors)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        r.render_batched(splats, cams, colors)
+    for _ in range(2):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps * 2):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / (reps * 2)
+    r.check()
+    n = len(cams)
+    return {"workload": f"batched: {splats.count} splats (gaussian layout), {n} random cameras at radius 6-12, "
+                        "fovy 40-75 deg, resolutions from 640x360 to 1920x1080",
+            "views_per_s": n / (batch_ms / 1e3), "plain_loop_views_per_s": n / (loop_ms / 1e3),
+            "speedup_vs_plain_loop": loop_ms / batch_ms, "ms_per_batch": batch_ms, "ms_plain_loop": loop_ms,
+            "lanes": choice.lanes, "slabs": list(choice.slabs), "graph": "one CUDA graph per batch (replayed)",
+            "form": "per-view pipelines spread over render lanes (sub-contexts + streams), forked/joined in one graph"}
 
 
 def run_reference(args):
@@ -355,6 +416,8 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clk,
     }
+    if not args.no_forms:
+        line["batched"] = batched_form(dev, quick=args.steps < 9)
     # cull_project, depth sort (histogram + 4 passes), then per depth slab: count, giant count, scan,
     # emit, giant emit, per-tile sort, raster
     launches_per_frame = 1 + 5 + 7 * DEFAULT_SLABS

@@ -193,6 +193,23 @@ gs_status gs_context_set_slabs(gs_context* context, uint32_t count, const uint32
 gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camera* camera,
                     const gs_target* target, const gs_frame_outputs* outputs, gs_stream stream);
 
+/* No counterpart in the reference (its viewer renders one camera per frame).  Renders n_views cameras
+ * of the same splats, view v into targets[v] (sizes may differ; each within the context's maxima), as
+ * gs_render would one by one.  The views are spread over the context's render lanes (see
+ * gs_context_set_batch_lanes): sub-contexts with their own scratch and stream, forked from `stream`
+ * and joined back into it with events, so the batch is ordered on `stream`, allocates nothing and can
+ * be captured in a CUDA graph as a whole.  With no lanes the views render one after another on
+ * `stream`.  gs_context_check afterwards reports every lane's errors and the summed statistics
+ * (tile_pairs: the largest). */
+gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32_t n_views,
+                            const gs_camera* cameras, const gs_target* targets, gs_stream stream);
+
+/* Creates `lanes` render lanes (0 ... GS_MAX_LANES) with this context's capacities, slab schedule and
+ * counting mode (later gs_context_reserve / set_slabs / set_count_fragments calls apply to them too).
+ * Synchronises the device and allocates: not for use inside a capture. */
+#define GS_MAX_LANES 16
+gs_status gs_context_set_batch_lanes(gs_context* context, uint32_t lanes);
+
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,

@@ -1,0 +1,116 @@
+"""GPU: the batched form (gs_render_batched) against single-view renders and the oracle."""
+
+import numpy as np
+import pytest
+
+from tests import scenes
+from vkgs_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n, seed, n_views, cam_seed):
+    import torch
+    from vkgs_gb300 import Camera, Splats, parse_ply
+
+    rows = syn.splat_rows(n, seed)
+    dev = torch.device("cuda", 0)
+    splats = parse_ply(torch.from_numpy(rows).to(dev), syn.ply_offsets())
+    specs = syn.random_cameras(n_views, seed=cam_seed)
+    cams = [Camera.from_spec(s) for s in specs]
+    colors = [torch.empty((c.height, c.width, 4), dtype=torch.float32, device=dev) for c in cams]
+    return rows, splats, specs, cams, colors
+
+
+@pytest.mark.parametrize("lanes", [0, 1, 3, 8])
+def test_batched_equals_single_view_renders(cuda, lanes):
+    """Every view of a batch is bit-identical to rendering that camera alone (same kernels, own scratch)."""
+    import torch
+    from vkgs_gb300 import Renderer
+
+    _, splats, specs, cams, colors = _setup(200_000, 11, 10, 501)
+    r = Renderer(200_000, 1920, 1080)
+    r.set_batch_lanes(lanes)
+    r.render_batched_checked(splats, cams, colors)
+    single = Renderer(200_000, 1920, 1080)
+    for cam, col in zip(cams, colors):
+        img, _ = single.render_checked(splats, cam)
+        assert torch.equal(img, col)
+
+
+def test_batched_matches_oracle(cuda, oracle):
+    from vkgs_gb300 import Renderer
+
+    rows, splats, specs, cams, colors = _setup(50_000, 12, 5, 502)
+    act = scenes.activated(oracle, rows)
+    r = Renderer(50_000, 1920, 1080)
+    r.set_batch_lanes(4)
+    r.render_batched_checked(splats, cams, colors)
+    for spec, col in zip(specs, colors):
+        c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=spec.width, height=spec.height)
+        o = oracle.render_frame(*act, scenes.oracle_camera(oracle, c))
+        err = np.abs(col.cpu().numpy().astype(np.float64) - o["image"]).max()
+        assert err <= 1.0 / 255.0, err
+
+
+def test_batched_graph_capture_replays(cuda):
+    """The whole batch captured in one CUDA graph replays to the same images (fresh look-back state per frame)."""
+    import torch
+    from vkgs_gb300 import Renderer
+
+    _, splats, specs, cams, colors = _setup(100_000, 13, 6, 503)
+    r = Renderer(100_000, 1920, 1080)
+    r.set_batch_lanes(3)
+    r.render_batched_checked(splats, cams, colors)
+    want = [c.clone() for c in colors]
+    for c in colors:
+        c.zero_()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        r.render_batched(splats, cams, colors)  # warm-up on the capture stream
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        r.render_batched(splats, cams, colors)
+    for _ in range(3):
+        for c in colors:
+            c.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip(colors, want):
+            assert torch.equal(a, b)
+    r.check()
+
+
+def test_batched_capacity_overflow_recovers(cuda):
+    import torch
+    from vkgs_gb300 import GsError, Renderer
+
+    _, splats, specs, cams, colors = _setup(100_000, 14, 4, 504)
+    r = Renderer(100_000, 1920, 1080, max_tile_pairs=2000)
+    r.set_batch_lanes(2)
+    r.render_batched(splats, cams, colors)
+    with pytest.raises(GsError) as e:
+        r.check()
+    assert e.value.status == 2 and e.value.stats["tile_pairs"] > 2000
+    stats = r.render_batched_checked(splats, cams, colors)
+    assert stats["visible_count"] > 0
+    single = Renderer(100_000, 1920, 1080)
+    img, _ = single.render_checked(splats, cams[0])
+    assert torch.equal(img, colors[0])
+
+
+def test_batched_rejects_bad_targets(cuda):
+    import torch
+    from vkgs_gb300 import GsError, Renderer
+
+    _, splats, specs, cams, colors = _setup(1000, 15, 2, 505)
+    r = Renderer(1000, 640, 360)
+    big = [c for c in cams if c.width > 640 or c.height > 360]
+    if big:
+        with pytest.raises(GsError):
+            r.render_batched(splats, big[:1], [torch.empty((big[0].height, big[0].width, 4), device="cuda")])
+    with pytest.raises(ValueError):
+        r.render_batched(splats, cams, colors[:1])

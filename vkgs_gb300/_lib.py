@@ -22,6 +22,7 @@ GS_ERROR_INTERNAL = 6
 GS_NUM_STAGES = 6
 GS_SORT_NOALLOC_MAX_COUNT = 1 << 20  # include/vkgs_gb300.h
 GS_MAX_SLABS = 4
+GS_MAX_LANES = 16
 STAGES = ("cull_project", "depth_sort", "bin", "emit", "tile_sort", "raster")
 
 
@@ -74,6 +75,9 @@ SIGNATURES = [
     ("gs_context_reserve", c_int, [c_void_p, POINTER(GsContextOptions)]),
     ("gs_context_set_count_fragments", c_int, [c_void_p, c_int]),
     ("gs_context_set_slabs", c_int, [c_void_p, c_uint32, POINTER(c_uint32)]),
+    ("gs_context_set_batch_lanes", c_int, [c_void_p, c_uint32]),
+    ("gs_render_batched", c_int,
+     [c_void_p, POINTER(GsSplats), c_uint32, POINTER(GsCamera), POINTER(GsTarget), c_void_p]),
     ("gs_render", c_int,
      [c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), POINTER(GsFrameOutputs), c_void_p]),
     ("gs_context_check", c_int, [c_void_p, c_void_p, POINTER(GsFrameStats)]),

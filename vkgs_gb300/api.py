@@ -233,6 +233,40 @@ class Renderer:
                                    ctypes.byref(outs), _stream(stream)), "gs_render")
         return color if color is not None else bgra8
 
+    def set_batch_lanes(self, lanes: int) -> None:
+        """Render lanes for render_batched (sub-contexts with their own scratch and stream; 0 = none)."""
+        _check(self._lib.gs_context_set_batch_lanes(self._h, int(lanes)), "gs_context_set_batch_lanes")
+
+    def render_batched(self, splats: Splats, cameras, colors, stream=None):
+        """Renders every camera into its own RGBA float32 target (H_v, W_v, 4) in one call (gs_render_batched)."""
+        n = len(cameras)
+        if len(colors) != n:
+            raise ValueError("one colour target per camera")
+        cams = (L.GsCamera * max(n, 1))()
+        targets = (L.GsTarget * max(n, 1))()
+        for v, (cam, col) in enumerate(zip(cameras, colors)):
+            _need_cuda(col, "colors[%d]" % v, torch.float32)
+            if tuple(col.shape) != (int(cam.height), int(cam.width), 4):
+                raise ValueError(f"colors[{v}] must be ({cam.height}, {cam.width}, 4)")
+            cams[v] = cam.struct()
+            targets[v] = L.GsTarget(_ptr(col), None, None)
+        s = splats.struct()
+        _check(self._lib.gs_render_batched(self._h, ctypes.byref(s), n, cams, targets, _stream(stream)),
+               "gs_render_batched")
+        return colors
+
+    def render_batched_checked(self, splats: Splats, cameras, colors, stream=None):
+        """render_batched + check; grows the tile-pair capacity and re-renders once if it overflowed."""
+        self.render_batched(splats, cameras, colors, stream)
+        try:
+            return self.check(stream)
+        except GsError as e:
+            if e.status != L.GS_ERROR_CAPACITY or not hasattr(e, "stats"):
+                raise
+            self.reserve(max_tile_pairs=int(e.stats["tile_pairs"] * 1.25) + 1024)
+            self.render_batched(splats, cameras, colors, stream)
+            return self.check(stream)
+
     def enable_timing(self, enable: bool = True) -> None:
         """Records CUDA events around each stage of every following frame (last 256 frames kept)."""
         _check(self._lib.gs_context_enable_timing(self._h, int(bool(enable))), "gs_context_enable_timing")

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/vkgs_gb300.h"
 #include "gs_internal.h"
@@ -91,6 +92,13 @@ struct gs_context {
   u32* tile_order = nullptr;
   float4* state_c = nullptr;  // running pixel sums between depth slabs
   float* state_t = nullptr;
+  // batched rendering: render lanes (sub-contexts with their own scratch and stream)
+  gs_context* lane[GS_MAX_LANES] = {};
+  cudaStream_t lane_stream[GS_MAX_LANES] = {};
+  cudaEvent_t lane_join[GS_MAX_LANES] = {};
+  cudaEvent_t batch_fork = nullptr;
+  u32 nlanes = 0;
+  bool last_batched = false;
   u32 slab_count = 2;  // nearest eighth of the visible splats, then the rest
   u32 slab_end[GS_MAX_SLABS] = {128, 1024, 1024, 1024};
   size_t status_bytes_begin = 0, status_bytes_end = 0;  // epoch-tagged region (zeroed on allocation)
@@ -104,16 +112,6 @@ struct gs_context {
   u32 timed_frames = 0;  // frames recorded since enabling (may exceed the ring)
 
   cudaEvent_t* frame_events(u32 frame) { return events + (size_t)(frame % kTimingRing) * kFrameEvents; }
-
-  u32 take_epochs(u32 k) {
-    if (epoch > 0xffffff00u) {  // wrap: clear every epoch-tagged status word once
-      cudaMemset(arena + status_bytes_begin, 0, status_bytes_end - status_bytes_begin);
-      epoch = 1;
-    }
-    const u32 e = epoch;
-    epoch += k;
-    return e;
-  }
 };
 
 struct gs_sorter {
@@ -373,8 +371,24 @@ gs_status gs_context_create(gs_context** out, const gs_context_options* o) {
   return GS_SUCCESS;
 }
 
+static void destroy_lanes(gs_context* c) {
+  if (c->nlanes) cudaDeviceSynchronize();
+  for (u32 l = 0; l < c->nlanes; ++l) {
+    gs_context_destroy(c->lane[l]);
+    if (c->lane_join[l]) cudaEventDestroy(c->lane_join[l]);
+    if (c->lane_stream[l]) cudaStreamDestroy(c->lane_stream[l]);
+    c->lane[l] = nullptr;
+    c->lane_join[l] = nullptr;
+    c->lane_stream[l] = nullptr;
+  }
+  if (c->batch_fork) cudaEventDestroy(c->batch_fork);
+  c->batch_fork = nullptr;
+  c->nlanes = 0;
+}
+
 void gs_context_destroy(gs_context* c) {
   if (!c) return;
+  destroy_lanes(c);
   if (c->arena) {
     cudaDeviceSynchronize();
     cudaFree(c->arena);
@@ -443,6 +457,10 @@ gs_status gs_context_reserve(gs_context* c, const gs_context_options* o) {
   const u32 w = std::max(c->max_width, o->max_width), h = std::max(c->max_height, o->max_height);
   u32 pairs = std::max(c->pair_capacity, o->max_tile_pairs);
   if (pairs > 0x3fffffffu) return GS_ERROR_CAPACITY;
+  for (u32 l = 0; l < c->nlanes; ++l) {
+    const gs_status ls = gs_context_reserve(c->lane[l], o);
+    if (ls != GS_SUCCESS) return ls;
+  }
   if (n == c->max_splats && w == c->max_width && h == c->max_height && pairs == c->pair_capacity) return GS_SUCCESS;
   if (cudaDeviceSynchronize() != cudaSuccess) return GS_ERROR_CUDA;
   return context_allocate(c, n, w, h, pairs);
@@ -455,12 +473,14 @@ gs_status gs_context_set_slabs(gs_context* c, uint32_t count, const uint32_t* en
   if (ends[count - 1] != 1024) return GS_ERROR_INVALID_ARGUMENT;
   c->slab_count = count;
   for (u32 i = 0; i < GS_MAX_SLABS; ++i) c->slab_end[i] = i < count ? ends[i] : 1024;
+  for (u32 l = 0; l < c->nlanes; ++l) gs_context_set_slabs(c->lane[l], count, ends);
   return GS_SUCCESS;
 }
 
 gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
   if (!c) return GS_ERROR_INVALID_ARGUMENT;
   c->count_fragments = enable ? 1 : 0;
+  for (u32 l = 0; l < c->nlanes; ++l) gs_context_set_count_fragments(c->lane[l], enable);
   return GS_SUCCESS;
 }
 
@@ -475,6 +495,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   if (s->count > 0x3fffffffu) return GS_ERROR_CAPACITY;
   gs_frame_outputs none{};
   const gs_frame_outputs& o = outs ? *outs : none;
+  c->last_batched = false;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const u32 n = s->count;
   const u32 W = cam->width, H = cam->height;
@@ -494,6 +515,9 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   if (ev) GS_TRY(cudaEventRecord(ev[i], st))
   GS_MARK(0);
   GS_TRY(cudaMemsetAsync(c->frame, 0, FW_WORDS * sizeof(u32), st));
+  // Look-back status words are cleared every frame and the frame's waits use fixed epochs (1: cull,
+  // 2-5: depth sort passes), so a frame captured in a CUDA graph replays correctly.
+  GS_TRY(cudaMemsetAsync(c->arena + c->status_bytes_begin, 0, c->status_bytes_end - c->status_bytes_begin, st));
   GS_TRY(cudaMemsetAsync(c->tile_done, 0, (size_t)(tiles + 31) / 32 * sizeof(u32), st));
   u32* key = o.keys ? o.keys : c->key;
   u32* index = o.index ? o.index : c->index;
@@ -511,7 +535,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   ca.visible_count = c->frame + FW_VISIBLE;
   ca.status = c->cull_status;
   ca.ticket = c->frame + FW_TICKET_CULL;
-  ca.epoch = c->take_epochs(1);
+  ca.epoch = 1;
   ca.err = c->err;
   ca.num_sms = c->num_sms;
   GS_TRY(launch_cull_project(fc, ca, st));
@@ -529,7 +553,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     ra.end_bit = 32;
     ra.control = c->radix_control;
     ra.status = c->radix_status;
-    ra.epoch = c->take_epochs(4);
+    ra.epoch = 2;
     ra.err = c->err;
     ra.num_sms = c->num_sms;
     GS_TRY(radix_sort(ra, st));  // 4 passes: sorted keys/index are back in key/index
@@ -568,6 +592,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     ba.slab_pairs = c->frame + FW_SLAB_PAIRS;
     ba.pair_total = c->frame + FW_PAIR_TOTAL;
     ba.pair_sum = reinterpret_cast<unsigned long long*>(c->frame + FW_PAIR_SUM);
+    ba.pair_peak = c->err + 1;
     ba.err = c->err;
     GS_TRY(launch_bin(ba, st, ev ? ev[e] : nullptr, ev ? ev[e + 1] : nullptr, c->num_sms));
     GS_MARK(e + 2);
@@ -602,6 +627,73 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   return GS_SUCCESS;
 }
 
+gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
+  if (!c || lanes > GS_MAX_LANES) return GS_ERROR_INVALID_ARGUMENT;
+  if (lanes == c->nlanes) return GS_SUCCESS;
+  destroy_lanes(c);
+  if (lanes == 0) return GS_SUCCESS;
+  if (cudaEventCreateWithFlags(&c->batch_fork, cudaEventDisableTiming) != cudaSuccess) return GS_ERROR_CUDA;
+  gs_context_options o{c->max_splats, c->max_width, c->max_height, c->pair_capacity};
+  for (u32 l = 0; l < lanes; ++l) {
+    gs_status st = gs_context_create(&c->lane[l], &o);
+    if (st == GS_SUCCESS && (cudaStreamCreateWithFlags(&c->lane_stream[l], cudaStreamNonBlocking) != cudaSuccess ||
+                             cudaEventCreateWithFlags(&c->lane_join[l], cudaEventDisableTiming) != cudaSuccess))
+      st = GS_ERROR_CUDA;
+    c->nlanes = l + 1;  // what exists so far is torn down on failure
+    if (st != GS_SUCCESS) {
+      destroy_lanes(c);
+      return st;
+    }
+    gs_context_set_slabs(c->lane[l], c->slab_count, c->slab_end);
+    gs_context_set_count_fragments(c->lane[l], c->count_fragments);
+  }
+  return GS_SUCCESS;
+}
+
+gs_status gs_render_batched(gs_context* c, const gs_splats* s, uint32_t n_views, const gs_camera* cams,
+                            const gs_target* targets, gs_stream stream) {
+  if (!c || !s || (n_views && (!cams || !targets))) return GS_ERROR_INVALID_ARGUMENT;
+  for (u32 v = 0; v < n_views; ++v) {  // validate everything before enqueueing anything
+    if (!targets[v].color_rgba32f && !targets[v].color_bgra8) return GS_ERROR_INVALID_ARGUMENT;
+    if (cams[v].width == 0 || cams[v].height == 0) return GS_ERROR_INVALID_ARGUMENT;
+    if (cams[v].width > c->max_width || cams[v].height > c->max_height) return GS_ERROR_CAPACITY;
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (c->nlanes == 0) {  // one after another on the caller's stream
+    for (u32 v = 0; v < n_views; ++v) {
+      const gs_status r = gs_render(c, s, &cams[v], &targets[v], nullptr, stream);
+      if (r != GS_SUCCESS) return r;
+    }
+    return GS_SUCCESS;
+  }
+  const u32 used = std::min(c->nlanes, std::max(n_views, 1u));
+  if (cudaEventRecord(c->batch_fork, st) != cudaSuccess) return GS_ERROR_CUDA;
+  for (u32 l = 0; l < used; ++l)
+    if (cudaStreamWaitEvent(c->lane_stream[l], c->batch_fork, 0) != cudaSuccess) return GS_ERROR_CUDA;
+  // Largest views first, each to the lane with the least work so far (work ~ pixels + a fixed cost per
+  // view), so the lanes finish together.
+  std::vector<u32> order(n_views);
+  for (u32 v = 0; v < n_views; ++v) order[v] = v;
+  const auto work = [&](u32 v) { return (double)cams[v].width * cams[v].height + 250000.0; };
+  std::stable_sort(order.begin(), order.end(), [&](u32 x, u32 y) { return work(x) > work(y); });
+  double load[GS_MAX_LANES] = {};
+  for (u32 v : order) {
+    u32 l = 0;
+    for (u32 k = 1; k < used; ++k)
+      if (load[k] < load[l]) l = k;
+    load[l] += work(v);
+    const gs_status r = gs_render(c->lane[l], s, &cams[v], &targets[v], nullptr,
+                                  reinterpret_cast<gs_stream>(c->lane_stream[l]));
+    if (r != GS_SUCCESS) return r;
+  }
+  for (u32 l = 0; l < used; ++l) {
+    if (cudaEventRecord(c->lane_join[l], c->lane_stream[l]) != cudaSuccess) return GS_ERROR_CUDA;
+    if (cudaStreamWaitEvent(st, c->lane_join[l], 0) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  c->last_batched = true;
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stats) {
   if (!c) return GS_ERROR_INVALID_ARGUMENT;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -621,6 +713,26 @@ gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stat
     std::memcpy(f, words + FW_FRAGMENTS, 16);
     stats->fragments = f[0];
     stats->fragments_blended = f[1];
+  }
+  u32 peak = 0;  // largest slab pair count since the last check (any frame, for capacity growth)
+  if (cudaMemcpy(&peak, c->err + 1, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return GS_ERROR_CUDA;
+  if (cudaMemset(c->err + 1, 0, 4) != cudaSuccess) return GS_ERROR_CUDA;
+  if (stats) stats->tile_pairs = std::max(stats->tile_pairs, peak);
+  for (u32 l = 0; l < c->nlanes; ++l) {  // batched frames: errors of every lane, stats summed (pairs: max)
+    gs_frame_stats ls{};
+    const gs_status r = gs_context_check(c->lane[l], stream, &ls);
+    if (r == GS_ERROR_DEVICE_TIMEOUT) e |= ERR_TIMEOUT;
+    else if (r == GS_ERROR_INTERNAL) e |= ERR_INTERNAL;
+    else if (r == GS_ERROR_CAPACITY) e |= ERR_CAPACITY;
+    else if (r != GS_SUCCESS) return r;
+    if (stats && c->last_batched) {
+      if (l == 0) *stats = gs_frame_stats{};
+      stats->visible_count += ls.visible_count;
+      stats->tile_pairs = std::max(stats->tile_pairs, ls.tile_pairs);
+      stats->fragments += ls.fragments;
+      stats->fragments_blended += ls.fragments_blended;
+      stats->pairs_emitted += ls.pairs_emitted;
+    }
   }
   if (e & ERR_TIMEOUT) return GS_ERROR_DEVICE_TIMEOUT;
   if (e & ERR_INTERNAL) return GS_ERROR_INTERNAL;

@@ -346,6 +346,7 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
   if (threadIdx.x == 0) {
     *a.slab_pairs = total;
     atomicMax(a.pair_total, total);
+    atomicMax(a.pair_peak, total);
     *a.pair_sum += total;
     if (total > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
   }

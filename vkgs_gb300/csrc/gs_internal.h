@@ -96,6 +96,7 @@ struct BinArgs {
   u32* slab_pairs;           // out: pairs this slab needs
   u32* pair_total;           // out: max over the frame's slabs (atomicMax)
   unsigned long long* pair_sum;  // out: sum over the frame's slabs
+  u32* pair_peak;            // out: max over every slab since the context was last checked (atomicMax)
   u32* err;
 };
 
