@@ -210,6 +210,47 @@ gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32
 #define GS_MAX_LANES 16
 gs_status gs_context_set_batch_lanes(gs_context* context, uint32_t lanes);
 
+/* ------------------------------------------------------------------------ */
+/* Differentiable path (no counterpart in the reference viewer)              */
+/* ------------------------------------------------------------------------ */
+
+/* Raw per-splat parameters, before activation (device pointers): what a trainer optimises.  The
+ * activation is parse_ply.comp's (s = exp(log_scale), q = quat / |quat|, cov3d = R diag(s^2) R^T,
+ * opacity = sigmoid(logit)); SH stay FP32. */
+typedef struct gs_train_params {
+  const float* means;          /* N x 3 */
+  const float* log_scales;     /* N x 3 */
+  const float* quats;          /* N x 4, (x, y, z, w), any nonzero length */
+  const float* opacity_logits; /* N */
+  const float* sh;             /* N x 48 FP32, [channel][16 coefficients] */
+  uint32_t count;
+} gs_train_params;
+
+/* Gradient buffers with the shapes of gs_train_params; gs_train_backward adds into them. */
+typedef struct gs_train_grads {
+  float* means;
+  float* log_scales;
+  float* quats;
+  float* opacity_logits;
+  float* sh;
+} gs_train_grads;
+
+/* The frame of gs_render (one depth slab, no caller depth) from raw parameters into an RGBA float
+ * target, keeping in the context what gs_train_backward needs: the activated splats, the tile lists,
+ * and per pixel its final transmittance and how many list entries it blended (each pixel stops
+ * exactly at transmittance 2^-24).  Valid until the context renders again. */
+gs_status gs_train_forward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
+                           float* color_rgba32f, gs_stream stream);
+
+/* Gradients of a loss with respect to the raw parameters, given dL/d(image) (H x W x 4 floats) for the
+ * last gs_train_forward of this context with the same params and camera.  The blend backward walks
+ * each tile's list in reverse from the stored final transmittance (no per-pixel lists are stored) and
+ * accumulates per-splat gradients warp-reduced, then atomically; the projection backward then runs per
+ * splat through conic -> 2D covariance -> scale / quaternion, SH -> coefficients, and back to the means
+ * (including the SH view direction).  Results are added into `grads`. */
+gs_status gs_train_backward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
+                            const float* grad_rgba32f, const gs_train_grads* grads, gs_stream stream);
+
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,

@@ -1,0 +1,87 @@
+"""GPU: the differentiable path (gs_train_forward / gs_train_backward behind a torch.autograd.Function)
+against the FP64 torch restatement of the reference (autograd) and the plain forward."""
+
+import numpy as np
+import pytest
+
+from tests import scenes
+from vkgs_gb300 import synthetic as syn
+from vkgs_gb300 import train_params as tp
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-3  # per parameter group: ||g_cuda - g_fp64|| / ||g_fp64||
+
+
+def _gpu_params(rows, f16_sh=False):
+    import torch
+
+    p = tp.from_rows(rows)
+    if f16_sh:
+        p["sh"] = p["sh"].astype(np.float16).astype(np.float32)
+    return {k: torch.tensor(v, device="cuda", requires_grad=True) for k, v in p.items()}
+
+
+@pytest.mark.parametrize("n,w,h,eye,seed", [(1000, 128, 128, (0.0, 0.0, 6.0), 3), (400, 96, 80, (1.5, 0.5, 4.0), 5)])
+def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed):
+    import torch
+    from oracle import torch_ref
+    from vkgs_gb300 import train
+
+    rows = syn.splat_rows(n, seed)
+    c = scenes.camera(oracle, eye, width=w, height=h)
+    act = scenes.activated(oracle, rows)
+    ocam = scenes.oracle_camera(oracle, c)
+    out = oracle.render_frame(*act, ocam)
+    _, rec = oracle.project(*act, out["index"], ocam)
+    weights = np.random.default_rng(seed).standard_normal((h, w, 4))
+
+    params = _gpu_params(rows)
+    from vkgs_gb300 import Renderer
+
+    r = Renderer(n, w, h)
+    img = train.render(params, scenes.product_camera(c), r)
+    (img * torch.tensor(weights, dtype=torch.float32, device="cuda")).sum().backward()
+
+    p64 = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True) for k, v in tp.from_rows(rows).items()}
+    img64 = torch_ref.render(p64["means"], p64["log_scales"], p64["quats"], p64["opacity_logits"], p64["sh"],
+                             torch_ref.camera_dict(c), out["index"], mask_records=rec)
+    (img64 * torch.tensor(weights)).sum().backward()
+
+    assert np.abs(img.detach().cpu().numpy() - img64.detach().numpy()).max() <= 1.0 / 255.0
+    for name in train.NAMES:
+        g = params[name].grad.double().cpu()
+        g64 = p64[name].grad
+        rel = float((g - g64).norm() / g64.norm())
+        assert rel <= GRAD_RTOL, (name, rel)
+
+
+def test_train_forward_equals_plain_forward(cuda, oracle):
+    """With binary16-representable SH the differentiable forward draws the plain forward's frame."""
+    import torch
+    from vkgs_gb300 import Renderer, Splats, parse_ply, train
+
+    rows = syn.splat_rows(50_000, 7)
+    rows_f16 = rows.copy()
+    off = syn.ply_offsets()
+    rows_f16[:, off[10:58]] = rows[:, off[10:58]].astype(np.float16).astype(np.float32)
+    c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=640, height=360)
+    cam = scenes.product_camera(c)
+    r = Renderer(50_000, 640, 360)
+    splats = parse_ply(torch.from_numpy(rows_f16).cuda(), off)
+    plain, _ = r.render_checked(splats, cam)
+    params = _gpu_params(rows_f16)
+    img = train.render(params, cam, Renderer(50_000, 640, 360))
+    assert float((img.detach() - plain).abs().max()) <= 1e-6
+
+
+def test_train_rejects_bad_shapes(cuda):
+    import torch
+    from vkgs_gb300 import Camera, Renderer, train
+
+    r = Renderer(10, 64, 64)
+    p = {k: torch.zeros((10,) + train.SHAPES[k], device="cuda") for k in train.NAMES}
+    p["sh"] = torch.zeros((10, 47), device="cuda")
+    cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=64, height=64))
+    with pytest.raises(ValueError):
+        train.render(p, cam, r)

@@ -59,6 +59,16 @@ class GsFrameStats(ctypes.Structure):
                 ("fragments_blended", c_uint64), ("pairs_emitted", c_uint64)]
 
 
+class GsTrainParams(ctypes.Structure):
+    _fields_ = [("means", c_void_p), ("log_scales", c_void_p), ("quats", c_void_p), ("opacity_logits", c_void_p),
+                ("sh", c_void_p), ("count", c_uint32)]
+
+
+class GsTrainGrads(ctypes.Structure):
+    _fields_ = [("means", c_void_p), ("log_scales", c_void_p), ("quats", c_void_p), ("opacity_logits", c_void_p),
+                ("sh", c_void_p)]
+
+
 # (name, restype, argtypes) for every entry point of include/vkgs_gb300.h
 SIGNATURES = [
     ("gs_status_string", c_char_p, [c_int]),
@@ -81,6 +91,9 @@ SIGNATURES = [
     ("gs_render", c_int,
      [c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), POINTER(GsFrameOutputs), c_void_p]),
     ("gs_context_check", c_int, [c_void_p, c_void_p, POINTER(GsFrameStats)]),
+    ("gs_train_forward", c_int, [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, c_void_p]),
+    ("gs_train_backward", c_int,
+     [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, POINTER(GsTrainGrads), c_void_p]),
     ("gs_context_enable_timing", c_int, [c_void_p, c_int]),
     ("gs_context_stage_times", c_int, [c_void_p, c_uint32, POINTER(c_float), POINTER(c_uint32)]),
     ("gs_ply_offsets_from_header", c_int,
@@ -124,4 +137,4 @@ def floats(values, n):
 
 
 __all__ = ["load", "LIB_PATH", "SIGNATURES", "GsSplats", "GsSplatBuffers", "GsCamera", "GsTarget", "GsFrameOutputs",
-           "GsContextOptions", "GsFrameStats", "status_string", "floats", "c_uint16"]
+           "GsContextOptions", "GsFrameStats", "GsTrainParams", "GsTrainGrads", "status_string", "floats", "c_uint16"]

@@ -90,6 +90,12 @@ struct gs_context {
   u32* tile_range = nullptr;
   u32* tile_done = nullptr;   // bitmap over tiles, cleared per frame
   u32* tile_order = nullptr;
+  // differentiable path
+  float* train_pos = nullptr;      // activated splats of the last gs_train_forward
+  float* train_cov = nullptr;
+  float* train_opacity = nullptr;
+  u32* train_nproc = nullptr;      // per pixel: list entries blended
+  float* grad_rec = nullptr;       // per splat blend gradients (kGradRec floats)
   float4* state_c = nullptr;  // running pixel sums between depth slabs
   float* state_t = nullptr;
   // batched rendering: render lanes (sub-contexts with their own scratch and stream)
@@ -142,6 +148,11 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->tile_range = cv.take<u32>((size_t)(max_tiles + 1) * 2);
     t->tile_done = cv.take<u32>((max_tiles + 31) / 32);
     t->tile_order = cv.take<u32>(max_tiles);
+    t->train_pos = cv.take<float>((size_t)n * 3);
+    t->train_cov = cv.take<float>((size_t)n * 6);
+    t->train_opacity = cv.take<float>(n);
+    t->train_nproc = cv.take<u32>((size_t)max_width * max_height);
+    t->grad_rec = cv.take<float>((size_t)n * kGradRec);
     t->state_c = cv.take<float4>((size_t)max_width * max_height);
     t->state_t = cv.take<float>((size_t)max_width * max_height);
     t->radix_control = cv.take<u32>(kRadixControlBytes / sizeof(u32));
@@ -484,15 +495,11 @@ gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
   return GS_SUCCESS;
 }
 
-gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, const gs_target* t,
-                    const gs_frame_outputs* outs, gs_stream stream) {
-  if (!c || !s || !cam || !t) return GS_ERROR_INVALID_ARGUMENT;
-  if (!t->color_rgba32f && !t->color_bgra8) return GS_ERROR_INVALID_ARGUMENT;
-  if (cam->width == 0 || cam->height == 0) return GS_ERROR_INVALID_ARGUMENT;
-  if (s->count && (!s->position || !s->cov3d || !s->opacity || !s->sh)) return GS_ERROR_INVALID_ARGUMENT;
-  if ((reinterpret_cast<uintptr_t>(s->sh) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
-  if (s->count > c->max_splats || cam->width > c->max_width || cam->height > c->max_height) return GS_ERROR_CAPACITY;
-  if (s->count > 0x3fffffffu) return GS_ERROR_CAPACITY;
+// One frame.  sh32 (the differentiable path): FP32 SH instead of s->sh, one depth slab, and the
+// training raster that stores per-pixel blend counts and final transmittance.
+static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh32, const gs_camera* cam,
+                              const gs_target* t, const gs_frame_outputs* outs, gs_stream stream) {
+  const bool train = sh32 != nullptr;
   gs_frame_outputs none{};
   const gs_frame_outputs& o = outs ? *outs : none;
   c->last_batched = false;
@@ -528,6 +535,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   ca.cov3d = s->cov3d;
   ca.opacity = s->opacity;
   ca.sh = s->sh;
+  ca.sh32 = sh32;
   ca.key = key;
   ca.index = index;
   ca.record = c->record;
@@ -564,7 +572,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
   GS_MARK(2);
 
   // Depth slabs, nearest first (one slab when nothing is visible).
-  const u32 slabs = n > 0 ? c->slab_count : 1;
+  const u32 slabs = (n > 0 && !train) ? c->slab_count : 1;
   if (ev) c->frame_slabs[(c->timed_frames - 1) % gs_context::kTimingRing] = slabs;
   for (u32 k = 0; k < slabs; ++k) {
     const int e = 3 + 4 * (int)k;
@@ -616,6 +624,7 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
     rr.tile_done = c->tile_done;
     rr.first = k == 0;
     rr.last = k + 1 == slabs;
+    rr.nproc = train ? c->train_nproc : nullptr;
     GS_TRY(launch_raster(rr, st));
     GS_MARK(e + 3);
   }
@@ -625,6 +634,96 @@ gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, con
 #undef GS_MARK
 #undef GS_TRY
   return GS_SUCCESS;
+}
+
+gs_status gs_render(gs_context* c, const gs_splats* s, const gs_camera* cam, const gs_target* t,
+                    const gs_frame_outputs* outs, gs_stream stream) {
+  if (!c || !s || !cam || !t) return GS_ERROR_INVALID_ARGUMENT;
+  if (!t->color_rgba32f && !t->color_bgra8) return GS_ERROR_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (s->count && (!s->position || !s->cov3d || !s->opacity || !s->sh)) return GS_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(s->sh) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (s->count > c->max_splats || cam->width > c->max_width || cam->height > c->max_height) return GS_ERROR_CAPACITY;
+  if (s->count > 0x3fffffffu) return GS_ERROR_CAPACITY;
+  return render_frame(c, s, nullptr, cam, t, outs, stream);
+}
+
+static gs_status check_train_params(const gs_context* c, const gs_train_params* p, const gs_camera* cam) {
+  if (!p || !cam) return GS_ERROR_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (p->count && (!p->means || !p->log_scales || !p->quats || !p->opacity_logits || !p->sh))
+    return GS_ERROR_INVALID_ARGUMENT;
+  if (((reinterpret_cast<uintptr_t>(p->quats) | reinterpret_cast<uintptr_t>(p->sh)) & 15u) != 0)
+    return GS_ERROR_INVALID_ARGUMENT;
+  if (p->count > c->max_splats || cam->width > c->max_width || cam->height > c->max_height) return GS_ERROR_CAPACITY;
+  return GS_SUCCESS;
+}
+
+gs_status gs_train_forward(gs_context* c, const gs_train_params* p, const gs_camera* cam, float* color,
+                           gs_stream stream) {
+  if (!c || !color) return GS_ERROR_INVALID_ARGUMENT;
+  const gs_status v = check_train_params(c, p, cam);
+  if (v != GS_SUCCESS) return v;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  TrainArgs ta{};
+  ta.means = p->means;
+  ta.log_scales = p->log_scales;
+  ta.quats = p->quats;
+  ta.opacity_logits = p->opacity_logits;
+  ta.sh = p->sh;
+  ta.n = p->count;
+  ta.position = c->train_pos;
+  ta.cov3d = c->train_cov;
+  ta.opacity = c->train_opacity;
+  if (launch_activate(ta, st) != cudaSuccess) return GS_ERROR_CUDA;
+  gs_splats s{c->train_pos, c->train_cov, c->train_opacity, nullptr, p->count};
+  gs_target t{color, nullptr, nullptr};
+  return render_frame(c, &s, p->sh, cam, &t, nullptr, stream);
+}
+
+gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
+                            const gs_train_grads* g, gs_stream stream) {
+  if (!c || !grad_rgba || !g) return GS_ERROR_INVALID_ARGUMENT;
+  const gs_status v = check_train_params(c, p, cam);
+  if (v != GS_SUCCESS) return v;
+  if (p->count && (!g->means || !g->log_scales || !g->quats || !g->opacity_logits || !g->sh))
+    return GS_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(g->quats) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const u32 W = cam->width, H = cam->height;
+  if (cudaMemsetAsync(c->grad_rec, 0, (size_t)p->count * kGradRec * sizeof(float), st) != cudaSuccess)
+    return GS_ERROR_CUDA;
+  RasterBackwardArgs rb{};
+  rb.tile_range = c->tile_range;
+  rb.pair_capacity = c->pair_capacity;
+  rb.pair_splat = c->pair_splat;
+  rb.record = c->record;
+  rb.width = W;
+  rb.height = H;
+  rb.tiles_x = (W + kTile - 1) / kTile;
+  rb.tiles_y = (H + kTile - 1) / kTile;
+  rb.state_t = c->state_t;
+  rb.nproc = c->train_nproc;
+  rb.grad_rgba = reinterpret_cast<const float4*>(grad_rgba);
+  rb.grad_rec = c->grad_rec;
+  if (launch_raster_backward(rb, st) != cudaSuccess) return GS_ERROR_CUDA;
+  FrameConst fc;
+  frame_constants(cam->projection, cam->view, cam->model, cam->camera_position, W, H, p->count, &fc);
+  TrainArgs ta{};
+  ta.means = p->means;
+  ta.log_scales = p->log_scales;
+  ta.quats = p->quats;
+  ta.opacity_logits = p->opacity_logits;
+  ta.sh = p->sh;
+  ta.n = p->count;
+  ta.grad_rec = c->grad_rec;
+  ta.record = c->record;
+  ta.g_means = g->means;
+  ta.g_log_scales = g->log_scales;
+  ta.g_quats = g->quats;
+  ta.g_opacity_logits = g->opacity_logits;
+  ta.g_sh = g->sh;
+  return from_cuda(launch_project_backward(fc, ta, st));
 }
 
 gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {

@@ -122,6 +122,47 @@ __device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp /* >= NT/
 
 // Per-frame constants of one camera (the Camera uniform + model push constant, pre-multiplied
 // where the reference multiplies per invocation).  Passed by value to the kernels.
+// parse_ply.comp:62-88: cov3d = rot * diag(s^2) * rot^T from log-scales and a (x, y, z, w) quaternion of
+// any length, in the shader's operation order (units including this must build without FMA contraction
+// for the result to be the restatement's bits).  cov = (00, 10, 20, 11, 21, 22).
+__device__ __forceinline__ void activate_cov3d(float ls0, float ls1, float ls2, float qx, float qy, float qz, float qw,
+                                               float cov[6]) {
+  const float s0 = expf(ls0), s1 = expf(ls1), s2 = expf(ls2);
+  const float len = sqrtf(((qx * qx + qy * qy) + qz * qz) + qw * qw);
+  qx = qx / len, qy = qy / len, qz = qz / len, qw = qw / len;
+  const float xx = qx * qx, yy = qy * qy, zz = qz * qz;
+  const float xy = qx * qy, xz = qx * qz, yz = qy * qz;
+  const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
+  float R[3][3];  // rot[col][row], column-major as in the shader
+  R[0][0] = 1.0f - 2.0f * (yy + zz);
+  R[0][1] = 2.0f * (xy + wz);
+  R[0][2] = 2.0f * (xz - wy);
+  R[1][0] = 2.0f * (xy - wz);
+  R[1][1] = 1.0f - 2.0f * (xx + zz);
+  R[1][2] = 2.0f * (yz + wx);
+  R[2][0] = 2.0f * (xz + wy);
+  R[2][1] = 2.0f * (yz - wx);
+  R[2][2] = 1.0f - 2.0f * (xx + yy);
+  const float S[3] = {s0 * s0, s1 * s1, s2 * s2};
+  // (rot * diag(S)) has columns S[j] * rot[j]; the shader's full product adds exact zeros, which
+  // leave every nonzero sum unchanged.
+  float T[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) T[j][i] = R[j][i] * S[j];
+  // cov = T * rot^T: cov[j][i] = (T[0][i] rot[0][j] + T[1][i] rot[1][j]) + T[2][i] rot[2][j]
+  const auto C = [&](int j, int i) { return (T[0][i] * R[0][j] + T[1][i] * R[1][j]) + T[2][i] * R[2][j]; };
+  cov[0] = C(0, 0);
+  cov[1] = C(1, 0);
+  cov[2] = C(2, 0);
+  cov[3] = C(1, 1);
+  cov[4] = C(2, 1);
+  cov[5] = C(2, 2);
+}
+
+__device__ __forceinline__ float activate_opacity(float logit) { return 1.0f / (1.0f + expf(-logit)); }
+
 struct FrameConst {
   float pvm[16];    // projection * view * model, glm operand order (rank.comp:32)
   float model[16];

@@ -134,12 +134,21 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
   const float b30 = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), b31 = -C32 * x * (4.0f * zz - xx - yy),
               b32 = C34 * z * (xx - yy), b33 = -C30 * x * (xx - 3.0f * yy);
   const uint4* shv = reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)id);
+  const float4* sh32 = a.sh32 ? reinterpret_cast<const float4*>(a.sh32 + 48 * (size_t)id) : nullptr;
   float color[3];
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     float g[16];
-    unpack_half8(__ldg(shv + 2 * ch), g);
-    unpack_half8(__ldg(shv + 2 * ch + 1), g + 8);
+    if (sh32) {  // FP32 coefficients (the differentiable path)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float4 v = __ldg(sh32 + 4 * ch + k);
+        g[4 * k] = v.x, g[4 * k + 1] = v.y, g[4 * k + 2] = v.z, g[4 * k + 3] = v.w;
+      }
+    } else {
+      unpack_half8(__ldg(shv + 2 * ch), g);
+      unpack_half8(__ldg(shv + 2 * ch + 1), g + 8);
+    }
     const float col = ((dot4(b00, b01, b02, b03, g[0], g[1], g[2], g[3]) +
                         dot4(b10, b11, b12, b13, g[4], g[5], g[6], g[7])) +
                        dot4(b20, b21, b22, b23, g[8], g[9], g[10], g[11])) +

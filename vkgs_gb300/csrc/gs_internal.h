@@ -49,6 +49,7 @@ struct CullArgs {
   u32* index;        // compacted ids
   float4* record;    // N x 4 float4 raster records, indexed by id
   float* inst_by_id; // optional N x 12 reference instance records, indexed by id
+  const float* sh32; // non-null: FP32 SH (N x 48) instead of sh (the differentiable path)
   u32* visible_count;
   u64* status;       // >= ceil(N / kCullTile) words
   u32* ticket;
@@ -120,10 +121,47 @@ struct RasterArgs {
   float* state_t;            // [H*W] running transmittance between slabs
   u32* tile_done;            // bitmap: tiles finished by an earlier slab (set here when one finishes)
   int first, last;           // first slab: no state to load; last slab: every tile resolves
+  u32* nproc;                // differentiable forward: per pixel, list entries blended (exact 2^-24 stop)
   unsigned long long* fragments;  // non-null: [0] covered fragments, [1] those met while T >= t_floor
                                   // (disables the early stop)
 };
 cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
+
+// ---- differentiable path (gs_train.cu, gs_raster.cu) ----
+constexpr u32 kGradRec = 12;  // per-splat blend gradients: dcx, dcy, dA, dB, dC (conic xx, yy, xy), do, dr, dg, db
+struct RasterBackwardArgs {
+  const u32* tile_range;
+  u32 pair_capacity;
+  const u32* pair_splat;
+  const float4* record;
+  u32 width, height, tiles_x, tiles_y;
+  const float* state_t;      // final transmittance per pixel
+  const u32* nproc;          // list entries blended per pixel
+  const float4* grad_rgba;   // dL/d(pixel)
+  float* grad_rec;           // [N][kGradRec], accumulated
+};
+cudaError_t launch_raster_backward(const RasterBackwardArgs& a, cudaStream_t stream);
+
+struct TrainArgs {
+  const float* means;
+  const float* log_scales;
+  const float* quats;
+  const float* opacity_logits;
+  const float* sh;
+  u32 n;
+  float* position;  // activated (forward)
+  float* cov3d;
+  float* opacity;
+  const float* grad_rec;  // backward input
+  const float4* record;   // drawn flags of this frame's records
+  float* g_means;         // backward outputs (added into)
+  float* g_log_scales;
+  float* g_quats;
+  float* g_opacity_logits;
+  float* g_sh;
+};
+cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream);
+cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, cudaStream_t stream);
 
 // ---- loader (gs_ply.cu) ----
 struct PlyOffsets {

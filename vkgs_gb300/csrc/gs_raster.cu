@@ -60,7 +60,10 @@ __device__ __forceinline__ u32 block_mask(const float4 q0, const float4 q1, cons
   return m;
 }
 
-template <bool DEPTH, bool COUNT>
+// TRAIN (the differentiable forward): every pixel stops exactly when its transmittance falls below
+// t_floor and records how many list entries it blended (nproc) and its final transmittance, which is
+// all the backward needs to walk the list in reverse.
+template <bool DEPTH, bool COUNT, bool TRAIN>
 __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
   __shared__ float4 s_q0[kRasterThreads];  // cx, cy, m00, m01
   __shared__ float4 s_q1[kRasterThreads];  // m10, m11, cz, opacity
@@ -91,7 +94,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
     cr = c.x, cg = c.y, cb = c.z, ca = c.w;
     T = a.state_t[pix];
   }
-  u32 frags = 0, needed = 0;
+  u32 frags = 0, needed = 0, blended = 0;
   const float kExp = -0.5f * 1.4426950408889634f;  // -log2(e)/2
   bool done = !inside || (!COUNT && T < a.t_floor);
   for (u32 hi = range.y; hi > range.x;) {
@@ -119,6 +122,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
         while (word) {
           const u32 j = 32u * k + (u32)(__ffs(word) - 1);
           word &= word - 1u;
+          if (TRAIN && T < a.t_floor) continue;  // this pixel has stopped
           const float4 q0 = s_q0[j], q1 = s_q1[j];
           const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
           const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
@@ -138,6 +142,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
           cb += w * q2.z;
           ca += w * al;
           T -= w;
+          if (TRAIN && cov) blended = range.y - hi + j + 1;  // processing index + 1 (0 = nearest)
         }
         // A warp whose 32 pixels are all below t_floor stops here (the remaining records can move no
         // channel of these pixels by more than t_floor).
@@ -162,6 +167,10 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
     if (lane == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
   }
   if (!inside) return;
+  if (TRAIN) {
+    a.nproc[pix] = blended;
+    a.state_t[pix] = T;
+  }
   if (!finished && !a.last) {  // a farther slab continues these pixels
     a.state_c[pix] = make_float4(cr, cg, cb, ca);
     a.state_t[pix] = T;
@@ -179,14 +188,140 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
   const u32 tiles = a.tiles_x * a.tiles_y;
   if (tiles == 0) return cudaSuccess;
   const bool depth = a.depth != nullptr, count = a.fragments != nullptr;
-  if (depth && count)
-    k_raster<true, true><<<tiles, kRasterThreads, 0, stream>>>(a);
+  if (a.nproc)
+    k_raster<false, false, true><<<tiles, kRasterThreads, 0, stream>>>(a);
+  else if (depth && count)
+    k_raster<true, true, false><<<tiles, kRasterThreads, 0, stream>>>(a);
   else if (depth)
-    k_raster<true, false><<<tiles, kRasterThreads, 0, stream>>>(a);
+    k_raster<true, false, false><<<tiles, kRasterThreads, 0, stream>>>(a);
   else if (count)
-    k_raster<false, true><<<tiles, kRasterThreads, 0, stream>>>(a);
+    k_raster<false, true, false><<<tiles, kRasterThreads, 0, stream>>>(a);
   else
-    k_raster<false, false><<<tiles, kRasterThreads, 0, stream>>>(a);
+    k_raster<false, false, false><<<tiles, kRasterThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Blend backward.  Per pixel the forward sum is RGB = sum_i a_i c_i T_i, A = sum_i a_i^2 T_i + T_end
+// over the nproc entries it blended (nearest first), T_i = prod_{j<i} (1 - a_j).  Walking those
+// entries in reverse from T_end, with T_i = T_{i+1} / (1 - a_i) and S the part of the loss gradient
+// carried by everything behind entry i (S starts at T_end dL/dA):
+//   dL/dc_i = a_i T_i dL/dRGB,   dL/da_i = T_i (c_i . dL/dRGB + 2 a_i dL/dA) - S / (1 - a_i),
+//   S += (a_i c_i . dL/dRGB + a_i^2 dL/dA) T_i,
+// and a_i = o exp(-q/2), q = d^T K d with K = M^T M the conic (M = rot_scale^-1, d = pixel - centre):
+//   dL/do = dL/da e^{-q/2},  dq/dcentre = -2 K d,  dq/dK = (dx^2, dy^2, 2 dx dy) for (Kxx, Kyy, Kxy).
+// Each warp (an 8x4 pixel block) walks only the records that can touch its block, reduces the 9
+// per-splat values over its 32 pixels with shuffles and adds them with one atomic per value.
+__global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const RasterBackwardArgs a) {
+  __shared__ float4 s_q0[kRasterThreads];
+  __shared__ float4 s_q1[kRasterThreads];
+  __shared__ float4 s_q2[kRasterThreads];
+  __shared__ u32 s_id[kRasterThreads];
+  __shared__ u32 s_bits[kWarps][kWarps];
+  __shared__ u32 s_nmax;
+  const u32 tile = blockIdx.x;
+  const u32 tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const u32 px = tx * kTile + (warp % kBlocksX) * kBlockW + lane % kBlockW;
+  const u32 py = ty * kTile + (warp / kBlocksX) * kBlockH + lane / kBlockW;
+  const bool inside = px < a.width && py < a.height;
+  const size_t pix = (size_t)py * a.width + px;
+  const float fx = __fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f;
+  const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
+  const u32 n = inside ? a.nproc[pix] : 0u;
+  float Tcur = inside ? a.state_t[pix] : 1.0f;
+  const float4 g = inside ? a.grad_rgba[pix] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float S = Tcur * g.w;
+  if (tid == 0) s_nmax = 0;
+  __syncthreads();
+  if (n) atomicMax(&s_nmax, n);
+  __syncthreads();
+  const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range)[tile];
+  const u32 hi = min(tr.y, a.pair_capacity);
+  const u32 first = hi - min(s_nmax, hi - min(tr.x, a.pair_capacity));  // farthest entry any pixel blended
+  const float sx = 2.0f / (float)a.width, sy = 2.0f / (float)a.height;
+  const float ox = (float)(2 * tx * kTile + 1) / (float)a.width - 1.0f;
+  const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
+  const float mx = 0.5f * sx, my = 0.5f * sy;
+  const float kExp = -0.5f * 1.4426950408889634f;
+  for (u32 lo = first; lo < hi; lo += kRasterThreads) {  // farthest first: the reverse of the forward
+    const u32 cnt = min((u32)kRasterThreads, hi - lo);
+    u32 mask = 0;
+    if (tid < cnt) {
+      const u32 id = a.pair_splat[lo + tid];
+      const float4* rec = a.record + 4 * (size_t)id;
+      const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
+      s_q0[tid] = q0;
+      s_q1[tid] = q1;
+      s_q2[tid] = rec[2];
+      s_id[tid] = id;
+      mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
+    }
+#pragma unroll
+    for (int b = 0; b < kWarps; ++b) {
+      const u32 bits = __ballot_sync(0xffffffffu, (mask >> b) & 1u);
+      if (lane == 0) s_bits[b][warp] = bits;
+    }
+    __syncthreads();
+    for (int k = 0; k < kWarps; ++k) {
+      u32 word = s_bits[warp][k];
+      while (word) {
+        const u32 j = 32u * k + (u32)(__ffs(word) - 1);
+        word &= word - 1u;
+        const u32 kproc = hi - 1 - (lo + j);  // processing index in the forward (0 = nearest)
+        const float4 q0 = s_q0[j], q1 = s_q1[j];
+        const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
+        const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
+        const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
+        const bool on = kproc < n && (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
+        float r[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (on) {
+          const float4 q2 = s_q2[j];
+          const float G = exp2f(kExp * (u * u + v * v));
+          const float al = q1.w * G;
+          const float inv = 1.0f / fmaxf(1.0f - al, 1e-6f);
+          const float Ti = Tcur * inv;
+          const float cg = q2.x * g.x + q2.y * g.y + q2.z * g.z;
+          const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
+          S += (al * cg + al * al * g.w) * Ti;
+          Tcur = Ti;
+          const float dLdq = -0.5f * al * dLda;
+          const float Kxx = q0.z * q0.z + q1.x * q1.x, Kyy = q0.w * q0.w + q1.y * q1.y;
+          const float Kxy = q0.z * q0.w + q1.x * q1.y;
+          r[0] = -2.0f * dLdq * (Kxx * dx + Kxy * dy);  // d/d centre x
+          r[1] = -2.0f * dLdq * (Kxy * dx + Kyy * dy);  // d/d centre y
+          r[2] = dLdq * dx * dx;                        // d/d Kxx
+          r[3] = dLdq * dy * dy;                        // d/d Kyy
+          r[4] = dLdq * 2.0f * dx * dy;                 // d/d Kxy
+          r[5] = dLda * G;                              // d/d opacity
+          const float w = al * Ti;
+          r[6] = w * g.x;
+          r[7] = w * g.y;
+          r[8] = w * g.z;
+        }
+        if (__any_sync(0xffffffffu, on)) {
+#pragma unroll
+          for (int t = 0; t < 9; ++t) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r[t] += __shfl_xor_sync(0xffffffffu, r[t], o);
+          }
+          if (lane < 9) {
+            float val = r[0];
+#pragma unroll
+            for (int t = 1; t < 9; ++t) val = lane == (u32)t ? r[t] : val;
+            atomicAdd(a.grad_rec + (size_t)s_id[j] * kGradRec + lane, val);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_raster_backward(const RasterBackwardArgs& a, cudaStream_t stream) {
+  const u32 tiles = a.tiles_x * a.tiles_y;
+  if (tiles == 0) return cudaSuccess;
+  k_raster_backward<<<tiles, kRasterThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,297 @@
+// gs_train.cu -- the differentiable path's per-splat kernels: activation (forward) and the projection
+// backward.  The blend backward is in gs_raster.cu.
+//
+// Forward chain (the reference's formulas, as in gs_ply.cu / gs_cull.cu):
+//   parse_ply.comp:62-88   s = exp(log_s), q = quat/|quat| (x, y, z, w), R(q), cov3d = R diag(s^2) R^T,
+//                          opacity = sigmoid(logit)
+//   projection.comp:95-116 pv = V M pos, Cv = A cov3d A^T (A = V3 M3), J2 = rows (-1/z, 0, x/z^2),
+//                          (0, -1/z, y/z^2), cov2d = P2 (J2 Cv J2^T) P2 + diag(1/W^2, 1/H^2)
+//   projection.comp:136-174 centre = (P pv).xy / w, colour = max(SH . basis(dir) + 0.5, 0),
+//                          dir = normalize(pos - M^-1 eye); the target clamps colour to 1
+//   splat.frag              alpha = o exp(-q/2), q = d^T K d, K = cov2d^-1 (= M^T M, M = rot_scale^-1)
+// The projection backward takes the per-splat blend gradients (centre, conic K, opacity, colour) and
+// applies the chain rule back to the raw parameters, recomputing the forward quantities it needs.
+#include "gs_common.cuh"
+#include "gs_internal.h"
+
+namespace gs {
+
+__device__ __forceinline__ void quat_rotation(float x, float y, float z, float w, float R[3][3]) {
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y,
+              wz = w * z;
+  R[0][0] = 1.0f - 2.0f * (yy + zz), R[0][1] = 2.0f * (xy - wz), R[0][2] = 2.0f * (xz + wy);
+  R[1][0] = 2.0f * (xy + wz), R[1][1] = 1.0f - 2.0f * (xx + zz), R[1][2] = 2.0f * (yz - wx);
+  R[2][0] = 2.0f * (xz - wy), R[2][1] = 2.0f * (yz + wx), R[2][2] = 1.0f - 2.0f * (xx + yy);
+}
+
+// parse_ply.comp's activation of the raw parameters (the same device code as k_parse_ply, so the records
+// of the differentiable forward are the plain path's for the same splats); SH stay FP32.
+__global__ void k_activate(const TrainArgs a) {
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
+    const float4 q = reinterpret_cast<const float4*>(a.quats)[id];
+    activate_cov3d(a.log_scales[3 * id], a.log_scales[3 * id + 1], a.log_scales[3 * id + 2], q.x, q.y, q.z, q.w,
+                   a.cov3d + 6 * (size_t)id);
+    a.opacity[id] = activate_opacity(a.opacity_logits[id]);
+    a.position[3 * id] = a.means[3 * id];
+    a.position[3 * id + 1] = a.means[3 * id + 1];
+    a.position[3 * id + 2] = a.means[3 * id + 2];
+  }
+}
+
+cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream) {
+  if (a.n == 0) return cudaSuccess;
+  k_activate<<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// Degree-3 SH basis B_k(d) and its gradient, the reference's coefficient order (projection.comp:140-163).
+__device__ __forceinline__ void sh_basis_grad(float x, float y, float z, float B[16], float dB[16][3]) {
+  const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f, C20 = 1.0925484305920792f,
+              C21 = 0.31539156525252005f, C22 = 0.5462742152960396f, C30 = 0.5900435899266435f,
+              C31 = 2.890611442640554f, C32 = 0.4570457994644658f, C33 = 0.3731763325901154f,
+              C34 = 1.445305721320277f;
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  B[0] = C0;
+  dB[0][0] = dB[0][1] = dB[0][2] = 0.0f;
+  B[1] = -C1 * y, dB[1][0] = 0.0f, dB[1][1] = -C1, dB[1][2] = 0.0f;
+  B[2] = C1 * z, dB[2][0] = 0.0f, dB[2][1] = 0.0f, dB[2][2] = C1;
+  B[3] = -C1 * x, dB[3][0] = -C1, dB[3][1] = 0.0f, dB[3][2] = 0.0f;
+  B[4] = C20 * xy, dB[4][0] = C20 * y, dB[4][1] = C20 * x, dB[4][2] = 0.0f;
+  B[5] = -C20 * yz, dB[5][0] = 0.0f, dB[5][1] = -C20 * z, dB[5][2] = -C20 * y;
+  B[6] = C21 * (2.0f * zz - xx - yy), dB[6][0] = -2.0f * C21 * x, dB[6][1] = -2.0f * C21 * y, dB[6][2] = 4.0f * C21 * z;
+  B[7] = -C20 * xz, dB[7][0] = -C20 * z, dB[7][1] = 0.0f, dB[7][2] = -C20 * x;
+  B[8] = C22 * (xx - yy), dB[8][0] = 2.0f * C22 * x, dB[8][1] = -2.0f * C22 * y, dB[8][2] = 0.0f;
+  B[9] = -C30 * y * (3.0f * xx - yy), dB[9][0] = -6.0f * C30 * xy, dB[9][1] = -C30 * (3.0f * xx - 3.0f * yy),
+  dB[9][2] = 0.0f;
+  B[10] = C31 * xy * z, dB[10][0] = C31 * yz, dB[10][1] = C31 * xz, dB[10][2] = C31 * xy;
+  B[11] = -C32 * y * (4.0f * zz - xx - yy), dB[11][0] = 2.0f * C32 * xy, dB[11][1] = -C32 * (4.0f * zz - xx - 3.0f * yy),
+  dB[11][2] = -8.0f * C32 * yz;
+  B[12] = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), dB[12][0] = -6.0f * C33 * xz, dB[12][1] = -6.0f * C33 * yz,
+  dB[12][2] = C33 * (6.0f * zz - 3.0f * xx - 3.0f * yy);
+  B[13] = -C32 * x * (4.0f * zz - xx - yy), dB[13][0] = -C32 * (4.0f * zz - 3.0f * xx - yy), dB[13][1] = 2.0f * C32 * xy,
+  dB[13][2] = -8.0f * C32 * xz;
+  B[14] = C34 * z * (xx - yy), dB[14][0] = 2.0f * C34 * xz, dB[14][1] = -2.0f * C34 * yz, dB[14][2] = C34 * (xx - yy);
+  B[15] = -C30 * x * (xx - 3.0f * yy), dB[15][0] = -C30 * (3.0f * xx - 3.0f * yy), dB[15][1] = 6.0f * C30 * xy,
+  dB[15][2] = 0.0f;
+}
+
+// m (column-major 4x4) as a row-major 3x3 / 4x4 element
+__device__ __forceinline__ float mel(const float* m, int r, int c) { return m[c * 4 + r]; }
+
+__global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
+    float gr[9];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      gr[k] = a.grad_rec[(size_t)id * kGradRec + k];
+      any |= gr[k] != 0.0f;
+    }
+    if (!any) continue;  // not in any tile list of this frame
+    // ---- forward quantities
+    const float ls0 = a.log_scales[3 * id], ls1 = a.log_scales[3 * id + 1], ls2 = a.log_scales[3 * id + 2];
+    const float sc[3] = {expf(ls0), expf(ls1), expf(ls2)};
+    const float4 q4 = reinterpret_cast<const float4*>(a.quats)[id];
+    const float qraw[4] = {q4.x, q4.y, q4.z, q4.w};
+    const float qlen = sqrtf(((q4.x * q4.x + q4.y * q4.y) + q4.z * q4.z) + q4.w * q4.w);
+    const float qn[4] = {q4.x / qlen, q4.y / qlen, q4.z / qlen, q4.w / qlen};
+    float R[3][3];
+    quat_rotation(qn[0], qn[1], qn[2], qn[3], R);
+    float Sg[3][3];  // cov3d
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        Sg[r][c] = R[r][0] * sc[0] * sc[0] * R[c][0] + R[r][1] * sc[1] * sc[1] * R[c][1] +
+                   R[r][2] * sc[2] * sc[2] * R[c][2];
+    const float ologit = a.opacity_logits[id];
+    const float o = 1.0f / (1.0f + expf(-ologit));
+    const float pos[3] = {a.means[3 * id], a.means[3 * id + 1], a.means[3 * id + 2]};
+    float A[3][3];  // V3 M3
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        A[r][c] = mel(fc.view, r, 0) * mel(fc.model, 0, c) + mel(fc.view, r, 1) * mel(fc.model, 1, c) +
+                  mel(fc.view, r, 2) * mel(fc.model, 2, c);
+    float p1[4], pv[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      p1[r] = mel(fc.model, r, 0) * pos[0] + mel(fc.model, r, 1) * pos[1] + mel(fc.model, r, 2) * pos[2] + mel(fc.model, r, 3);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      pv[r] = mel(fc.view, r, 0) * p1[0] + mel(fc.view, r, 1) * p1[1] + mel(fc.view, r, 2) * p1[2] + mel(fc.view, r, 3) * p1[3];
+    float Cv[3][3], T3[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) T3[r][c] = A[r][0] * Sg[0][c] + A[r][1] * Sg[1][c] + A[r][2] * Sg[2][c];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Cv[r][c] = T3[r][0] * A[c][0] + T3[r][1] * A[c][1] + T3[r][2] * A[c][2];
+    const float x = pv[0], y = pv[1], z = pv[2];
+    const float J[2][3] = {{-1.0f / z, 0.0f, x / z / z}, {0.0f, -1.0f / z, y / z / z}};
+    float JC[2][3], C2[2][2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) JC[r][c] = J[r][0] * Cv[0][c] + J[r][1] * Cv[1][c] + J[r][2] * Cv[2][c];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) C2[r][c] = JC[r][0] * J[c][0] + JC[r][1] * J[c][1] + JC[r][2] * J[c][2];
+    const float P2[2][2] = {{mel(fc.proj, 0, 0), mel(fc.proj, 0, 1)}, {mel(fc.proj, 1, 0), mel(fc.proj, 1, 1)}};
+    float PC[2][2], S2[2][2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) PC[r][c] = P2[r][0] * C2[0][c] + P2[r][1] * C2[1][c];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) S2[r][c] = PC[r][0] * P2[0][c] + PC[r][1] * P2[1][c];
+    S2[0][0] += fc.lpx;
+    S2[1][1] += fc.lpy;
+    const float sa = S2[0][0], sb = S2[1][1], scc = 0.5f * (S2[0][1] + S2[1][0]);
+    const float det = sa * sb - scc * scc;
+    const float K[2][2] = {{sb / det, -scc / det}, {-scc / det, sa / det}};
+    float pc[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      pc[r] = mel(fc.proj, r, 0) * pv[0] + mel(fc.proj, r, 1) * pv[1] + mel(fc.proj, r, 2) * pv[2] + mel(fc.proj, r, 3) * pv[3];
+    const float nx = pc[0] / pc[3], ny = pc[1] / pc[3];
+    const float dv[3] = {pos[0] - fc.cam_m[0], pos[1] - fc.cam_m[1], pos[2] - fc.cam_m[2]};
+    const float dl = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    const float dir[3] = {dv[0] / dl, dv[1] / dl, dv[2] / dl};
+    float B[16], dB[16][3];
+    sh_basis_grad(dir[0], dir[1], dir[2], B, dB);
+
+    // ---- colour -> SH and view direction
+    const float* shp = a.sh + 48 * (size_t)id;
+    float* gsh = a.g_sh + 48 * (size_t)id;
+    float gdir[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      float col = 0.5f;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) col += B[k] * shp[16 * ch + k];
+      const float gc = (col > 0.0f && col < 1.0f) ? gr[6 + ch] : 0.0f;  // max(., 0) and the target's clamp
+      if (gc == 0.0f) continue;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        gsh[16 * ch + k] += B[k] * gc;
+        const float w = shp[16 * ch + k] * gc;
+        gdir[0] += w * dB[k][0], gdir[1] += w * dB[k][1], gdir[2] += w * dB[k][2];
+      }
+    }
+    const float dd = dir[0] * gdir[0] + dir[1] * gdir[1] + dir[2] * gdir[2];
+    float gpos[3] = {(gdir[0] - dir[0] * dd) / dl, (gdir[1] - dir[1] * dd) / dl, (gdir[2] - dir[2] * dd) / dl};
+
+    // ---- conic -> cov2d -> C2 -> (J, Cv) -> cov3d
+    const float Gb[2][2] = {{gr[2], 0.5f * gr[4]}, {0.5f * gr[4], gr[3]}};
+    float KG[2][2], gS2[2][2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) KG[r][c] = K[r][0] * Gb[0][c] + K[r][1] * Gb[1][c];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) gS2[r][c] = -(KG[r][0] * K[0][c] + KG[r][1] * K[1][c]);
+    float tP[2][2], gC2[2][2];  // gC2 = P2^T gS2 P2^T
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) tP[r][c] = P2[0][r] * gS2[0][c] + P2[1][r] * gS2[1][c];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) gC2[r][c] = tP[r][0] * P2[c][0] + tP[r][1] * P2[c][1];
+    float gCv[3][3];  // J^T gC2 J
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        gCv[r][c] = J[0][r] * (gC2[0][0] * J[0][c] + gC2[0][1] * J[1][c]) +
+                    J[1][r] * (gC2[1][0] * J[0][c] + gC2[1][1] * J[1][c]);
+    float gJ[2][3];  // (gC2 + gC2^T) J Cv
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float s0 = gC2[r][0] + gC2[0][r], s1 = gC2[r][1] + gC2[1][r];
+        gJ[r][c] = s0 * JC[0][c] + s1 * JC[1][c];
+      }
+    const float iz2 = 1.0f / (z * z), iz3 = iz2 / z;
+    float gpv[3] = {gJ[0][2] * iz2, gJ[1][2] * iz2,
+                    (gJ[0][0] + gJ[1][1]) * iz2 - 2.0f * (x * gJ[0][2] + y * gJ[1][2]) * iz3};
+    // centre: (P pv).xy / w
+    const float iw = 1.0f / pc[3];
+    const float gpc[4] = {gr[0] * iw, gr[1] * iw, 0.0f, -(gr[0] * nx + gr[1] * ny) * iw};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      gpv[c] += mel(fc.proj, 0, c) * gpc[0] + mel(fc.proj, 1, c) * gpc[1] + mel(fc.proj, 2, c) * gpc[2] +
+                mel(fc.proj, 3, c) * gpc[3];
+    // pv = V M pos: the linear part is A
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gpos[c] += A[0][c] * gpv[0] + A[1][c] * gpv[1] + A[2][c] * gpv[2];
+    float gS[3][3];  // A^T gCv A
+    float tA[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) tA[r][c] = A[0][r] * gCv[0][c] + A[1][r] * gCv[1][c] + A[2][r] * gCv[2][c];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gS[r][c] = tA[r][0] * A[0][c] + tA[r][1] * A[1][c] + tA[r][2] * A[2][c];
+
+    // ---- cov3d = (R S)(R S)^T -> scale, rotation -> quaternion
+    float gsc[3] = {0.0f, 0.0f, 0.0f}, gR[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        // d cov / d M_ri with M = R diag(s): (gS + gS^T) M
+        const float gM = (gS[r][0] + gS[0][r]) * R[0][i] * sc[i] + (gS[r][1] + gS[1][r]) * R[1][i] * sc[i] +
+                         (gS[r][2] + gS[2][r]) * R[2][i] * sc[i];
+        gsc[i] += gM * R[r][i];
+        gR[r][i] = gM * sc[i];
+      }
+    const float qx = qn[0], qy = qn[1], qz = qn[2], qw = qn[3];
+    float gq[4];
+    gq[0] = 2.0f * (qy * (gR[0][1] + gR[1][0]) + qz * (gR[0][2] + gR[2][0]) + qw * (gR[2][1] - gR[1][2])) -
+            4.0f * qx * (gR[1][1] + gR[2][2]);
+    gq[1] = 2.0f * (qx * (gR[0][1] + gR[1][0]) + qw * (gR[0][2] - gR[2][0]) + qz * (gR[1][2] + gR[2][1])) -
+            4.0f * qy * (gR[0][0] + gR[2][2]);
+    gq[2] = 2.0f * (qw * (gR[1][0] - gR[0][1]) + qx * (gR[0][2] + gR[2][0]) + qy * (gR[1][2] + gR[2][1])) -
+            4.0f * qz * (gR[0][0] + gR[1][1]);
+    gq[3] = 2.0f * (qz * (gR[1][0] - gR[0][1]) + qy * (gR[0][2] - gR[2][0]) + qx * (gR[2][1] - gR[1][2]));
+    const float qd = qn[0] * gq[0] + qn[1] * gq[1] + qn[2] * gq[2] + qn[3] * gq[3];
+    float4* gq4 = reinterpret_cast<float4*>(a.g_quats) + id;
+    float4 acc = *gq4;
+    acc.x += (gq[0] - qn[0] * qd) / qlen;
+    acc.y += (gq[1] - qn[1] * qd) / qlen;
+    acc.z += (gq[2] - qn[2] * qd) / qlen;
+    acc.w += (gq[3] - qn[3] * qd) / qlen;
+    *gq4 = acc;
+    (void)qraw;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      a.g_log_scales[3 * id + i] += gsc[i] * sc[i];
+      a.g_means[3 * id + i] += gpos[i];
+    }
+    a.g_opacity_logits[id] += gr[5] * o * (1.0f - o);
+  }
+}
+
+cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, cudaStream_t stream) {
+  if (a.n == 0) return cudaSuccess;
+  k_project_backward<<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(fc, a);
+  return cudaGetLastError();
+}
+
+}  // namespace gs
