@@ -688,7 +688,8 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
   if (v != GS_SUCCESS) return v;
   if (p->count && (!g->means || !g->log_scales || !g->quats || !g->opacity_logits || !g->sh))
     return GS_ERROR_INVALID_ARGUMENT;
-  if ((reinterpret_cast<uintptr_t>(g->quats) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (((reinterpret_cast<uintptr_t>(g->quats) | reinterpret_cast<uintptr_t>(g->sh)) & 15u) != 0)
+    return GS_ERROR_INVALID_ARGUMENT;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const u32 W = cam->width, H = cam->height;
   if (cudaMemsetAsync(c->grad_rec, 0, (size_t)p->count * kGradRec * sizeof(float), st) != cudaSuccess)

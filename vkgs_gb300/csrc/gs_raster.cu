@@ -210,8 +210,33 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
 //   S += (a_i c_i . dL/dRGB + a_i^2 dL/dA) T_i,
 // and a_i = o exp(-q/2), q = d^T K d with K = M^T M the conic (M = rot_scale^-1, d = pixel - centre):
 //   dL/do = dL/da e^{-q/2},  dq/dcentre = -2 K d,  dq/dK = (dx^2, dy^2, 2 dx dy) for (Kxx, Kyy, Kxy).
+// Sums 9 values over the warp by recursive halving: after three halving steps each group of four lanes
+// holds one of v[0..7] (index = lane bits 4, 3, 2), finished by two more shuffles; v[8] is summed
+// alone.  14 shuffles instead of 45.  Lane 4k (k < 8) returns the total of v[k], lane 0 also *v8.
+__device__ __forceinline__ float warp_sum9(float v[9], float* v8) {
+  const u32 lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int half = 4, off = 16; half >= 1; half >>= 1, off >>= 1) {
+    const bool up = (lane & (u32)off) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const float send = up ? v[i] : v[i + half];
+      const float keep = up ? v[i + half] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  float t = v[0];
+  t += __shfl_xor_sync(0xffffffffu, t, 2);
+  t += __shfl_xor_sync(0xffffffffu, t, 1);
+  float e = v[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  *v8 = e;
+  return t;
+}
+
 // Each warp (an 8x4 pixel block) walks only the records that can touch its block, reduces the 9
-// per-splat values over its 32 pixels with shuffles and adds them with one atomic per value.
+// per-splat values over its 32 pixels (warp_sum9) and adds them with one atomic per value.
 __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const RasterBackwardArgs a) {
   __shared__ float4 s_q0[kRasterThreads];
   __shared__ float4 s_q1[kRasterThreads];
@@ -232,6 +257,9 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
   float Tcur = inside ? a.state_t[pix] : 1.0f;
   const float4 g = inside ? a.grad_rgba[pix] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float S = Tcur * g.w;
+  u32 wmax = n;  // the most list entries any pixel of this warp blended
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
   if (tid == 0) s_nmax = 0;
   __syncthreads();
   if (n) atomicMax(&s_nmax, n);
@@ -269,6 +297,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
         const u32 j = 32u * k + (u32)(__ffs(word) - 1);
         word &= word - 1u;
         const u32 kproc = hi - 1 - (lo + j);  // processing index in the forward (0 = nearest)
+        if (kproc >= wmax) continue;           // behind every pixel of this warp (warp-uniform)
         const float4 q0 = s_q0[j], q1 = s_q1[j];
         const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
         const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
@@ -279,7 +308,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
           const float4 q2 = s_q2[j];
           const float G = exp2f(kExp * (u * u + v * v));
           const float al = q1.w * G;
-          const float inv = 1.0f / fmaxf(1.0f - al, 1e-6f);
+          const float inv = __fdividef(1.0f, fmaxf(1.0f - al, 1e-6f));
           const float Ti = Tcur * inv;
           const float cg = q2.x * g.x + q2.y * g.y + q2.z * g.z;
           const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
@@ -300,17 +329,14 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
           r[8] = w * g.z;
         }
         if (__any_sync(0xffffffffu, on)) {
-#pragma unroll
-          for (int t = 0; t < 9; ++t) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) r[t] += __shfl_xor_sync(0xffffffffu, r[t], o);
+          float r8;
+          const float sum = warp_sum9(r, &r8);
+          float* dst = a.grad_rec + (size_t)s_id[j] * kGradRec;
+          if ((lane & 3u) == 0) {
+            const u32 idx = ((lane >> 4) & 1u) * 4u + ((lane >> 3) & 1u) * 2u + ((lane >> 2) & 1u);
+            atomicAdd(dst + idx, sum);
           }
-          if (lane < 9) {
-            float val = r[0];
-#pragma unroll
-            for (int t = 1; t < 9; ++t) val = lane == (u32)t ? r[t] : val;
-            atomicAdd(a.grad_rec + (size_t)s_id[j] * kGradRec + lane, val);
-          }
+          if (lane == 0) atomicAdd(dst + 8, r8);
         }
       }
     }

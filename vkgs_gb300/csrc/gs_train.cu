@@ -82,13 +82,16 @@ __device__ __forceinline__ float mel(const float* m, int r, int c) { return m[c 
 __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
   const u32 stride = gridDim.x * blockDim.x;
   for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
-    float gr[9];
+    float gr[12];
+    const float4* __restrict__ g4 = reinterpret_cast<const float4*>(a.grad_rec + (size_t)id * kGradRec);
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      gr[k] = a.grad_rec[(size_t)id * kGradRec + k];
-      any |= gr[k] != 0.0f;
+    for (int k = 0; k < 3; ++k) {
+      const float4 v = __ldg(g4 + k);
+      gr[4 * k] = v.x, gr[4 * k + 1] = v.y, gr[4 * k + 2] = v.z, gr[4 * k + 3] = v.w;
     }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) any |= gr[k] != 0.0f;
     if (!any) continue;  // not in any tile list of this frame
     // ---- forward quantities
     const float ls0 = a.log_scales[3 * id], ls1 = a.log_scales[3 * id + 1], ls2 = a.log_scales[3 * id + 2];
@@ -169,21 +172,32 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
     float B[16], dB[16][3];
     sh_basis_grad(dir[0], dir[1], dir[2], B, dB);
 
-    // ---- colour -> SH and view direction
-    const float* shp = a.sh + 48 * (size_t)id;
-    float* gsh = a.g_sh + 48 * (size_t)id;
+    // ---- colour -> SH and view direction (one channel's 16 coefficients at a time, as float4s)
+    const float4* __restrict__ shp = reinterpret_cast<const float4*>(a.sh + 48 * (size_t)id);
+    float4* __restrict__ gsh = reinterpret_cast<float4*>(a.g_sh + 48 * (size_t)id);
     float gdir[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
+      float c16[16];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float4 v = __ldg(shp + 4 * ch + k);
+        c16[4 * k] = v.x, c16[4 * k + 1] = v.y, c16[4 * k + 2] = v.z, c16[4 * k + 3] = v.w;
+      }
       float col = 0.5f;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) col += B[k] * shp[16 * ch + k];
+      for (int k = 0; k < 16; ++k) col += B[k] * c16[k];
       const float gc = (col > 0.0f && col < 1.0f) ? gr[6 + ch] : 0.0f;  // max(., 0) and the target's clamp
       if (gc == 0.0f) continue;
 #pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float4 acc = gsh[4 * ch + k];
+        acc.x += B[4 * k] * gc, acc.y += B[4 * k + 1] * gc, acc.z += B[4 * k + 2] * gc, acc.w += B[4 * k + 3] * gc;
+        gsh[4 * ch + k] = acc;
+      }
+#pragma unroll
       for (int k = 0; k < 16; ++k) {
-        gsh[16 * ch + k] += B[k] * gc;
-        const float w = shp[16 * ch + k] * gc;
+        const float w = c16[k] * gc;
         gdir[0] += w * dB[k][0], gdir[1] += w * dB[k][1], gdir[2] += w * dB[k][2];
       }
     }

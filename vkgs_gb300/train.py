@@ -33,14 +33,23 @@ def _train_params(tensors) -> L.GsTrainParams:
     return L.GsTrainParams(*[_ptr(t) for t in tensors], n)
 
 
-def forward(renderer: Renderer, tensors, camera: Camera, stream=None) -> torch.Tensor:
-    """gs_train_forward into a new (H, W, 4) image; grows the pair capacity once if it overflowed."""
+def forward(renderer: Renderer, tensors, camera: Camera, stream=None, check: bool | None = None) -> torch.Tensor:
+    """gs_train_forward into a new (H, W, 4) image.
+
+    The first call on a renderer (or check=True) synchronises, checks the device error word and grows the
+    pair capacity once if it overflowed; later calls stay asynchronous (no host sync inside a training
+    step) and report errors at the next Renderer.check()."""
     p = _train_params(tensors)
     img = torch.empty((int(camera.height), int(camera.width), 4), dtype=torch.float32, device=tensors[0].device)
     cam = camera.struct()
     lib = renderer._lib
     _check(lib.gs_train_forward(renderer._h, ctypes.byref(p), ctypes.byref(cam), _ptr(img), _stream(stream)),
            "gs_train_forward")
+    if check is None:
+        check = not getattr(renderer, "_train_sized", False)
+    if not check:
+        return img
+    renderer._train_sized = True
     try:
         renderer.check(stream)
     except GsError as e:
