@@ -222,6 +222,61 @@ def batched_form(dev, quick: bool = False):
             "form": "per-view pipelines spread over render lanes (sub-contexts + streams), forked/joined in one graph"}
 
 
+def differentiation_form(dev, quick: bool = False):
+    """fwd+bwd through the autograd Function (200k splats, 800x800, L1 loss to a target rendered from
+    perturbed parameters: means + N(0, 0.01), SH DC + N(0, 0.05)) against the plain forward of the same frame."""
+    import numpy as np
+    import torch
+    from vkgs_gb300 import Camera, Renderer, parse_ply, synthetic as syn, train, train_params as tp
+
+    rows, off, specs = syn.workload("grad")
+    cam = Camera.from_spec(specs[0])
+    raw = tp.from_rows(rows)
+    params = {k: torch.tensor(v, device=dev, requires_grad=True) for k, v in raw.items()}
+    rng = np.random.default_rng(4)
+    pert = dict(raw)
+    pert["means"] = raw["means"] + rng.normal(0.0, 0.01, raw["means"].shape).astype(np.float32)
+    sh = raw["sh"].reshape(-1, 3, 16).copy()
+    sh[:, :, 0] += rng.normal(0.0, 0.05, sh[:, :, 0].shape).astype(np.float32)
+    pert["sh"] = sh.reshape(-1, 48)
+    r = Renderer(rows.shape[0], cam.width, cam.height)
+    with torch.no_grad():
+        target = train.render({k: torch.tensor(v, device=dev) for k, v in pert.items()}, cam, r).clone()
+    splats = parse_ply(torch.from_numpy(rows).to(dev), off)
+    plain = Renderer(rows.shape[0], cam.width, cam.height)
+    plain.render_checked(splats, cam)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5 if quick else 30
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    fwd_ms = timed(lambda: plain.render(splats, cam))
+
+    def step():
+        for t in params.values():
+            t.grad = None
+        loss = (train.render(params, cam, r) - target).abs().mean()
+        loss.backward()
+
+    step_ms = timed(step)
+    r.check()
+    plain.check()
+    return {"workload": f"fwd+bwd: {rows.shape[0]} splats (gaussian layout), 800x800, L1 loss to a perturbed-parameter "
+                        "target, gradients for means, log-scales, quaternions, opacity logits and FP32 SH",
+            "fwd_bwd_it_per_s": 1e3 / step_ms, "ms_fwd_bwd": step_ms, "ms_forward": fwd_ms,
+            "fwd_bwd_over_forward": step_ms / fwd_ms,
+            "form": "torch.autograd.Function over gs_train_forward / gs_train_backward (loss and autograd included)"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -418,6 +473,7 @@ def run_ours(args):
     }
     if not args.no_forms:
         line["batched"] = batched_form(dev, quick=args.steps < 9)
+        line["differentiation"] = differentiation_form(dev, quick=args.steps < 9)
     # cull_project, depth sort (histogram + 4 passes), then per depth slab: count, giant count, scan,
     # emit, giant emit, per-tile sort, raster
     launches_per_frame = 1 + 5 + 7 * DEFAULT_SLABS
