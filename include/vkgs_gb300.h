@@ -251,6 +251,18 @@ gs_status gs_train_forward(gs_context* context, const gs_train_params* params, c
 gs_status gs_train_backward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
                             const float* grad_rgba32f, const gs_train_grads* grads, gs_stream stream);
 
+/* No counterpart in the reference's API: the per-frame loop of Engine::Run (engine.cc:551-601) as a CUDA
+ * graph.  gs_viewer_create captures one gs_render of `splats` into `target` with this context (no frame
+ * outputs, the target's resolution fixed) on an internal stream; gs_viewer_frame then rewrites the
+ * camera constants of the graph's cull node (the only kernel that reads the camera) and launches the
+ * graph on `stream`.  Camera width/height must equal the creation camera's.  The context must not be
+ * used for other renders while the viewer exists, and timing must be disabled. */
+typedef struct gs_viewer gs_viewer;
+gs_status gs_viewer_create(gs_viewer** viewer, gs_context* context, const gs_splats* splats, const gs_camera* camera,
+                           const gs_target* target);
+gs_status gs_viewer_frame(gs_viewer* viewer, const gs_camera* camera, gs_stream stream);
+void gs_viewer_destroy(gs_viewer* viewer);
+
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,

@@ -1,0 +1,45 @@
+"""GPU: the viewer loop (one CUDA graph per frame, camera rewritten in the graph) against gs_render."""
+
+import pytest
+
+from vkgs_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def test_viewer_frames_equal_direct_renders(cuda):
+    import torch
+    from vkgs_gb300 import Camera, Renderer, Viewer, parse_ply
+
+    rows = syn.splat_rows(300_000, 21, "shell")
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    specs = syn.circle_cameras(width=800, height=450)
+    cams = [Camera.from_spec(s) for s in specs]
+    direct = Renderer(300_000, 800, 450)
+    want = [direct.render_checked(splats, c)[0].clone() for c in cams]
+    r = Renderer(300_000, 800, 450)
+    for c in cams:  # size the pair capacity before the graph is captured
+        r.render_checked(splats, c)
+    color = torch.zeros((450, 800, 4), device="cuda")
+    v = Viewer(r, splats, cams[0], color)
+    for _ in range(2):
+        for c, w in zip(cams, want):
+            img = v.frame(c)
+            torch.cuda.synchronize()
+            assert torch.equal(img, w)
+    r.check()
+    v.close()
+
+
+def test_viewer_rejects_other_resolution(cuda):
+    import torch
+    from vkgs_gb300 import Camera, GsError, Renderer, Viewer, parse_ply
+
+    rows = syn.splat_rows(1000, 22)
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=320, height=180))
+    r = Renderer(1000, 640, 360)
+    v = Viewer(r, splats, cam, torch.zeros((180, 320, 4), device="cuda"))
+    with pytest.raises(GsError):
+        v.frame(Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=640, height=360)))
+    v.close()

@@ -4,8 +4,8 @@ The compute lives in ``libvkgs_gb300.so`` (C ABI: ``include/vkgs_gb300.h``); thi
 for PyTorch callers.  See ``vkgs_gb300.api`` for the tensor-level calls.
 """
 
-from .api import (Camera, GsError, Renderer, Sorter, Splats, load, look_at, orbit_eye, parse_ply, perspective,
-                  ply_header, write_ply)
+from .api import (Camera, GsError, Renderer, Sorter, Splats, Viewer, load, look_at, orbit_eye, parse_ply,
+                  perspective, ply_header, write_ply)
 
-__all__ = ["Camera", "GsError", "Renderer", "Sorter", "Splats", "load", "look_at", "orbit_eye", "parse_ply",
-           "perspective", "ply_header", "write_ply"]
+__all__ = ["Camera", "GsError", "Renderer", "Sorter", "Splats", "Viewer", "load", "look_at", "orbit_eye",
+           "parse_ply", "perspective", "ply_header", "write_ply"]

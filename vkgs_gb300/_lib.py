@@ -86,6 +86,9 @@ SIGNATURES = [
     ("gs_context_set_count_fragments", c_int, [c_void_p, c_int]),
     ("gs_context_set_slabs", c_int, [c_void_p, c_uint32, POINTER(c_uint32)]),
     ("gs_context_set_batch_lanes", c_int, [c_void_p, c_uint32]),
+    ("gs_viewer_create", c_int, [POINTER(c_void_p), c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget)]),
+    ("gs_viewer_frame", c_int, [c_void_p, POINTER(GsCamera), c_void_p]),
+    ("gs_viewer_destroy", None, [c_void_p]),
     ("gs_render_batched", c_int,
      [c_void_p, POINTER(GsSplats), c_uint32, POINTER(GsCamera), POINTER(GsTarget), c_void_p]),
     ("gs_render", c_int,

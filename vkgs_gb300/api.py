@@ -306,6 +306,44 @@ class Renderer:
             return img, self.check(kw.get("stream"))
 
 
+# ----------------------------------------------------------------------------------------- viewer loop
+
+class Viewer:
+    """The viewer's per-frame loop as a CUDA graph (gs_viewer_*): one captured frame of `renderer` drawing
+    `splats` into `color`; frame(camera) updates the camera inside the graph and launches it.  The
+    renderer must not render anything else while the viewer exists."""
+
+    def __init__(self, renderer: Renderer, splats: Splats, camera: Camera, color: torch.Tensor):
+        _need_cuda(color, "color", torch.float32)
+        if tuple(color.shape) != (int(camera.height), int(camera.width), 4):
+            raise ValueError("color must be (H, W, 4)")
+        self._lib = renderer._lib
+        self.renderer, self.splats, self.color = renderer, splats, color  # keep the buffers alive
+        self._s = splats.struct()
+        cam = camera.struct()
+        target = L.GsTarget(_ptr(color), None, None)
+        h = ctypes.c_void_p()
+        _check(self._lib.gs_viewer_create(ctypes.byref(h), renderer._h, ctypes.byref(self._s), ctypes.byref(cam),
+                                          ctypes.byref(target)), "gs_viewer_create")
+        self._h = h
+
+    def frame(self, camera: Camera, stream=None) -> torch.Tensor:
+        cam = camera.struct()
+        _check(self._lib.gs_viewer_frame(self._h, ctypes.byref(cam), _stream(stream)), "gs_viewer_frame")
+        return self.color
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gs_viewer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ----------------------------------------------------------------------------------------- sorter
 
 class Sorter:

@@ -727,6 +727,84 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
   return from_cuda(launch_project_backward(fc, ta, st));
 }
 
+// ------------------------------------------------------------------ viewer loop (CUDA graph per frame)
+
+struct gs_viewer {
+  gs_context* ctx = nullptr;
+  cudaStream_t capture = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t cull = nullptr;  // kernel node whose FrameConst is rewritten per frame
+  CullArgs cull_args{};
+  cudaKernelNodeParams cull_params{};
+  u32 width = 0, height = 0, count = 0;
+};
+
+void gs_viewer_destroy(gs_viewer* v) {
+  if (!v) return;
+  if (v->exec) cudaGraphExecDestroy(v->exec);
+  if (v->graph) cudaGraphDestroy(v->graph);
+  if (v->capture) cudaStreamDestroy(v->capture);
+  delete v;
+}
+
+gs_status gs_viewer_create(gs_viewer** out, gs_context* c, const gs_splats* s, const gs_camera* cam,
+                           const gs_target* t) {
+  if (!out || !c || !s || !cam || !t) return GS_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (c->timing) return GS_ERROR_INVALID_ARGUMENT;
+  gs_viewer* v = new (std::nothrow) gs_viewer();
+  if (!v) return GS_ERROR_OUT_OF_MEMORY;
+  v->ctx = c;
+  v->width = cam->width;
+  v->height = cam->height;
+  v->count = s->count;
+  const auto fail = [&](gs_status st) {
+    gs_viewer_destroy(v);
+    return st;
+  };
+  if (cudaStreamCreateWithFlags(&v->capture, cudaStreamNonBlocking) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  if (cudaStreamBeginCapture(v->capture, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  const gs_status r = gs_render(c, s, cam, t, nullptr, reinterpret_cast<gs_stream>(v->capture));
+  const cudaError_t e = cudaStreamEndCapture(v->capture, &v->graph);
+  if (r != GS_SUCCESS) return fail(r);
+  if (e != cudaSuccess) return fail(GS_ERROR_CUDA);
+  size_t count = 0;
+  if (cudaGraphGetNodes(v->graph, nullptr, &count) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (count && cudaGraphGetNodes(v->graph, nodes.data(), &count) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType type;
+    if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp{};
+    if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) continue;
+    if (kp.func != cull_project_kernel()) continue;
+    v->cull = node;
+    v->cull_params = kp;
+    v->cull_args = *reinterpret_cast<const CullArgs*>(kp.kernelParams[1]);
+  }
+  if (s->count && !v->cull) return fail(GS_ERROR_INTERNAL);
+  if (cudaGraphInstantiate(&v->exec, v->graph, 0) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  *out = v;
+  return GS_SUCCESS;
+}
+
+gs_status gs_viewer_frame(gs_viewer* v, const gs_camera* cam, gs_stream stream) {
+  if (!v || !cam) return GS_ERROR_INVALID_ARGUMENT;
+  if (cam->width != v->width || cam->height != v->height) return GS_ERROR_INVALID_ARGUMENT;
+  if (v->cull) {
+    FrameConst fc;
+    frame_constants(cam->projection, cam->view, cam->model, cam->camera_position, v->width, v->height, v->count, &fc);
+    CullArgs ca = v->cull_args;
+    void* args[2] = {&fc, &ca};
+    cudaKernelNodeParams kp = v->cull_params;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    if (cudaGraphExecKernelNodeSetParams(v->exec, v->cull, &kp) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  return from_cuda(cudaGraphLaunch(v->exec, reinterpret_cast<cudaStream_t>(stream)));
+}
+
 gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
   if (!c || lanes > GS_MAX_LANES) return GS_ERROR_INVALID_ARGUMENT;
   if (lanes == c->nlanes) return GS_SUCCESS;

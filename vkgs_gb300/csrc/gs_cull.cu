@@ -54,6 +54,9 @@ __device__ __forceinline__ void unpack_half8(const uint4 q, float f[8]) {
   }
 }
 
+// SH32: FP32 coefficients (the differentiable path) instead of binary16 -- a separate instantiation, so
+// the plain path's kernel keeps its register count.
+template <bool SH32>
 __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, float x0, float y0, float z0) {
   // direction for SH in model space (projection.comp:85-87); normalize = v / sqrt(dot(v, v))
   const float ddx = x0 - fc.cam_m[0], ddy = y0 - fc.cam_m[1], ddz = z0 - fc.cam_m[2];
@@ -134,12 +137,12 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
   const float b30 = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), b31 = -C32 * x * (4.0f * zz - xx - yy),
               b32 = C34 * z * (xx - yy), b33 = -C30 * x * (xx - 3.0f * yy);
   const uint4* shv = reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)id);
-  const float4* sh32 = a.sh32 ? reinterpret_cast<const float4*>(a.sh32 + 48 * (size_t)id) : nullptr;
+  const float4* sh32 = SH32 ? reinterpret_cast<const float4*>(a.sh32 + 48 * (size_t)id) : nullptr;
   float color[3];
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     float g[16];
-    if (sh32) {  // FP32 coefficients (the differentiable path)
+    if (SH32) {  // FP32 coefficients (the differentiable path)
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const float4 v = __ldg(sh32 + 4 * ch + k);
@@ -173,6 +176,7 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
   }
 }
 
+template <bool SH32>
 __global__ __launch_bounds__(kCullThreads) void k_cull_project(const FrameConst fc, const CullArgs a) {
   __shared__ u32 s_cnt[kCullItems][kCullThreads / 32];
   __shared__ u32 s_off[kCullItems][kCullThreads / 32];
@@ -234,17 +238,22 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_project(const FrameConst 
     }
 #pragma unroll 1
     for (u32 k = 0; k < kCullItems; ++k)
-      if (vis[k]) project_splat(fc, a, p * kCullTile + k * kCullThreads + tid, px[k], py[k], pz[k]);
+      if (vis[k]) project_splat<SH32>(fc, a, p * kCullTile + k * kCullThreads + tid, px[k], py[k], pz[k]);
     __syncthreads();
   }
 }
+
+const void* cull_project_kernel() { return reinterpret_cast<const void*>(&k_cull_project<false>); }
 
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream) {
   if (fc.n == 0) return cudaSuccess;
   const u32 parts = (fc.n + kCullTile - 1) / kCullTile;
   const int sms = a.num_sms > 0 ? a.num_sms : 1;
   const u32 grid = min(parts, (u32)sms * 8u);
-  k_cull_project<<<grid, kCullThreads, 0, stream>>>(fc, a);
+  if (a.sh32)
+    k_cull_project<true><<<grid, kCullThreads, 0, stream>>>(fc, a);
+  else
+    k_cull_project<false><<<grid, kCullThreads, 0, stream>>>(fc, a);
   return cudaGetLastError();
 }
 

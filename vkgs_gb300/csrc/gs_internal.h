@@ -58,6 +58,7 @@ struct CullArgs {
   int num_sms;
 };
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
+const void* cull_project_kernel();  // the plain path's cull kernel (the only one reading the camera)
 
 // Gathers instance records into sorted order and writes the indirect draw arguments.
 cudaError_t launch_instances(const u32* index, const u32* visible_count, const float* inst_by_id, u32 n,
