@@ -177,7 +177,7 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
 }
 
 template <bool SH32>
-__global__ __launch_bounds__(kCullThreads) void k_cull_project(const FrameConst fc, const CullArgs a) {
+__global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameConst fc, const CullArgs a) {
   __shared__ u32 s_cnt[kCullItems][kCullThreads / 32];
   __shared__ u32 s_off[kCullItems][kCullThreads / 32];
   __shared__ u32 s_base;

@@ -64,7 +64,7 @@ __device__ __forceinline__ u32 block_mask(const float4 q0, const float4 q1, cons
 // t_floor and records how many list entries it blended (nproc) and its final transmittance, which is
 // all the backward needs to walk the list in reverse.
 template <bool DEPTH, bool COUNT, bool TRAIN>
-__global__ __launch_bounds__(kRasterThreads) void k_raster(const RasterArgs a) {
+__global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a) {
   __shared__ float4 s_q0[kRasterThreads];  // cx, cy, m00, m01
   __shared__ float4 s_q1[kRasterThreads];  // m10, m11, cz, opacity
   __shared__ float4 s_q2[kRasterThreads];  // r, g, b, -
