@@ -164,7 +164,7 @@ typedef struct gs_frame_stats {
                                  invocations of the reference's draw; only with
                                  gs_context_set_count_fragments(1) */
   uint64_t fragments_blended; /* of those, the ones met front to back while the pixel's transmittance
-                                 was still >= 2^-24 (the blend work actually needed) */
+                                 was still >= the transmittance floor (the blend work actually needed) */
   uint64_t pairs_emitted;     /* (splat, tile) pairs binned and sorted over all slabs of the last frame */
 } gs_frame_stats;
 
@@ -175,16 +175,23 @@ void gs_context_destroy(gs_context* context);
 /* Grows the reserved scratch (never shrinks).  Synchronises the device; not for use inside capture. */
 gs_status gs_context_reserve(gs_context* context, const gs_context_options* options);
 
+/* No counterpart in the reference (which blends every fragment).  A pixel stops blending once its
+ * transmittance T falls below t_floor: everything behind it can then move no channel by more than T,
+ * so the image differs from the full blend by less than t_floor per channel.  Default 1e-4 (the
+ * threshold of the original 3DGS rasteriser; 39x inside a 1/255 tolerance); valid range
+ * (0, 1/255].  The differentiable path always uses 2^-24. */
+gs_status gs_context_set_transmittance_floor(gs_context* context, float t_floor);
+
 /* Makes every following gs_render also count fragments (slower; for statistics and tests). */
 gs_status gs_context_set_count_fragments(gs_context* context, int enable);
 
 /* No counterpart in the reference (a scheduling knob of this implementation).  gs_render bins,
  * sorts and blends the depth-sorted splats in up to GS_MAX_SLABS slabs, nearest first, carrying
  * every pixel's blend state from one slab to the next; a 16x16 tile whose pixels all fall below
- * transmittance 2^-24 is finished and receives no pairs from the slabs behind.  ends[i] is the
+ * the transmittance floor is finished and receives no pairs from the slabs behind.  ends[i] is the
  * cumulative share of the visible splats in slabs 0..i, in 1/1024 units, strictly increasing,
  * with ends[count-1] = 1024; {1024} is a single slab.  The image is the same for every schedule up
- * to the 2^-24 early stop. */
+ * to the early stop. */
 #define GS_MAX_SLABS 4
 gs_status gs_context_set_slabs(gs_context* context, uint32_t count, const uint32_t* ends);
 

@@ -330,6 +330,31 @@ def test_slab_schedules(cuda, oracle, ends):
         assert g["stats"]["pairs_emitted"] == one
 
 
+@pytest.mark.parametrize("t_floor,bound", [(1e-4, 1e-4 + 2e-6), (2.0 ** -24, 2e-6), (1.0 / 255.0, 1.0 / 255.0 + 2e-6)])
+def test_transmittance_floor_bounds_the_image_error(cuda, oracle, t_floor, bound):
+    """Stopping a pixel at transmittance t_floor changes no channel by more than t_floor (+ FP32 noise)."""
+    from vkgs_gb300 import Renderer
+
+    rows = syn.splat_rows(300_000, 8, "shell")
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.0, 1.0, 8.0), width=800, height=450)
+    r = Renderer(300_000, 800, 450)
+    r.set_transmittance_floor(t_floor)
+    g = render_gpu(act, c, count_fragments=False, renderer=r)
+    o = render_cpu(oracle, act, c)
+    err = assert_parity(g, o, fragments=False)
+    assert err <= bound, err
+
+
+def test_transmittance_floor_rejects_bad_values(cuda):
+    from vkgs_gb300 import GsError, Renderer
+
+    r = Renderer(100, 64, 64)
+    for bad in (0.0, -1.0, 0.01, float("nan")):
+        with pytest.raises(GsError):
+            r.set_transmittance_floor(bad)
+
+
 def test_slab_schedule_rejects_bad_input(cuda):
     from vkgs_gb300 import GsError, Renderer
 

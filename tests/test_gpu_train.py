@@ -68,6 +68,7 @@ def test_train_forward_equals_plain_forward(cuda, oracle):
     c = scenes.camera(oracle, (0.0, 0.0, 6.0), width=640, height=360)
     cam = scenes.product_camera(c)
     r = Renderer(50_000, 640, 360)
+    r.set_transmittance_floor(2.0 ** -24)  # the differentiable path's floor
     splats = parse_ply(torch.from_numpy(rows_f16).cuda(), off)
     plain, _ = r.render_checked(splats, cam)
     params = _gpu_params(rows_f16)

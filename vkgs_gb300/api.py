@@ -191,6 +191,11 @@ class Renderer:
         arr = (ctypes.c_uint32 * len(ends))(*ends)
         _check(self._lib.gs_context_set_slabs(self._h, len(ends), arr), "gs_context_set_slabs")
 
+    def set_transmittance_floor(self, t_floor: float = 1e-4) -> None:
+        """Early stop: a pixel stops blending once its transmittance is below t_floor (image error < t_floor)."""
+        _check(self._lib.gs_context_set_transmittance_floor(self._h, float(t_floor)),
+               "gs_context_set_transmittance_floor")
+
     def count_fragments(self, enable: bool = True) -> None:
         _check(self._lib.gs_context_set_count_fragments(self._h, int(bool(enable))), "count_fragments")
 

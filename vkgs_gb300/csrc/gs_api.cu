@@ -66,6 +66,7 @@ struct gs_context {
   int num_sms = 1;
   u32 max_splats = 0, max_width = 0, max_height = 0, max_tiles = 0, pair_capacity = 0;
   int count_fragments = 0;
+  float t_floor = 1e-4f;  // early stop: remaining contributions move no channel by more than this
   u32 epoch = 1;
   char* arena = nullptr;
   size_t arena_bytes = 0;
@@ -488,6 +489,13 @@ gs_status gs_context_set_slabs(gs_context* c, uint32_t count, const uint32_t* en
   return GS_SUCCESS;
 }
 
+gs_status gs_context_set_transmittance_floor(gs_context* c, float t_floor) {
+  if (!c || !(t_floor > 0.0f) || !(t_floor <= 1.0f / 255.0f)) return GS_ERROR_INVALID_ARGUMENT;
+  c->t_floor = t_floor;
+  for (u32 l = 0; l < c->nlanes; ++l) gs_context_set_transmittance_floor(c->lane[l], t_floor);
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
   if (!c) return GS_ERROR_INVALID_ARGUMENT;
   c->count_fragments = enable ? 1 : 0;
@@ -617,7 +625,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     rr.out_rgba = t->color_rgba32f;
     rr.out_bgra = reinterpret_cast<uchar4*>(t->color_bgra8);
     rr.depth = t->depth;
-    rr.t_floor = 5.9604645e-08f;  // 2^-24
+    rr.t_floor = train ? 5.9604645e-08f : c->t_floor;  // the differentiable path keeps 2^-24
     rr.fragments = c->count_fragments ? reinterpret_cast<unsigned long long*>(c->frame + FW_FRAGMENTS) : nullptr;
     rr.state_c = c->state_c;
     rr.state_t = c->state_t;
@@ -824,6 +832,7 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
     }
     gs_context_set_slabs(c->lane[l], c->slab_count, c->slab_end);
     gs_context_set_count_fragments(c->lane[l], c->count_fragments);
+    gs_context_set_transmittance_floor(c->lane[l], c->t_floor);
   }
   return GS_SUCCESS;
 }
