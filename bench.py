@@ -219,12 +219,97 @@ def batched_form(dev, quick: bool = False):
     batch_ms = e0.elapsed_time(e1) / (reps * 2)
     r.check()
     n = len(cams)
-    return {"workload": f"batched: {splats.count} splats (gaussian layout), {n} random cameras at radius 6-12, "
+    return {"workload": f"batched: {splats.count} splats (shell layout), {n} random cameras at radius 6-12, "
                         "fovy 40-75 deg, resolutions from 640x360 to 1920x1080",
             "views_per_s": n / (batch_ms / 1e3), "plain_loop_views_per_s": n / (loop_ms / 1e3),
             "speedup_vs_plain_loop": loop_ms / batch_ms, "ms_per_batch": batch_ms, "ms_plain_loop": loop_ms,
             "lanes": choice.lanes, "slabs": list(choice.slabs), "graph": "one CUDA graph per batch (replayed)",
             "form": "per-view pipelines spread over render lanes (sub-contexts + streams), forked/joined in one graph"}
+
+
+def _perturbed(raw: dict, seed: int = 4) -> dict:
+    """The target's parameters: means + N(0, 0.01), SH DC + N(0, 0.05)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    pert = dict(raw)
+    pert["means"] = raw["means"] + rng.normal(0.0, 0.01, raw["means"].shape).astype(np.float32)
+    sh = raw["sh"].reshape(-1, 3, 16).copy()
+    sh[:, :, 0] += rng.normal(0.0, 0.05, sh[:, :, 0].shape).astype(np.float32)
+    pert["sh"] = sh.reshape(-1, 48)
+    return pert
+
+
+def batched_differentiation_form(dev, quick: bool = False):
+    """fwd+bwd of 16 views per step (3M splats, resolutions from {800x800, 1264x832, 1600x900}, L1 loss to
+    targets rendered from perturbed parameters): the batched autograd Function, gradients of all views
+    accumulated into one per-splat buffer, against a per-view loop of the one-view Function."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer, synthetic as syn, train, train_params as tp
+
+    rows, _, specs = syn.workload("batched_grad")
+    raw = tp.from_rows(rows)
+    n = rows.shape[0]
+    del rows
+    cams = [Camera.from_spec(sp) for sp in specs]
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    params = {k: torch.tensor(v, device=dev, requires_grad=True) for k, v in raw.items()}
+    mw, mh = max(c.width for c in cams), max(c.height for c in cams)
+    r = Renderer(n, mw, mh)
+    r.set_batch_lanes(len(cams))
+    with torch.no_grad():
+        pert = {k: torch.tensor(v, device=dev) for k, v in _perturbed(raw).items()}
+        targets = [t.clone() for t in train.render_batched(pert, cams, r)]
+        del pert
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3 if quick else 10
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def step():
+        for t in params.values():
+            t.grad = None
+        imgs = train.render_batched(params, cams, r)
+        loss = sum((img - tgt).abs().mean() for img, tgt in zip(imgs, targets)) / len(cams)
+        loss.backward()
+
+    torch.cuda.reset_peak_memory_stats()
+    step_ms = timed(step)
+    r.check()
+    free1, _ = torch.cuda.mem_get_info()
+    # device memory outside torch's caching allocator (the renderer's arenas, CUDA context) + torch's peak
+    outside = (total - free1) - torch.cuda.memory_reserved()
+    peak_gb = (outside + torch.cuda.max_memory_reserved()) / 1e9
+    single = Renderer(n, mw, mh)
+
+    def loop():
+        for t in params.values():
+            t.grad = None
+        for cam, tgt in zip(cams, targets):
+            ((train.render(params, cam, single) - tgt).abs().mean() / len(cams)).backward()
+
+    loop_ms = timed(loop)
+    single.check()
+    res = sorted({f"{c.width}x{c.height}" for c in cams})
+    return {"workload": f"batched fwd+bwd: {n} splats (shell layout), {len(cams)} views per step at "
+                        f"{', '.join(res)}, L1 loss to perturbed-parameter targets, gradients of all views "
+                        "accumulated into one per-splat buffer",
+            "fwd_bwd_it_per_s": 1e3 / step_ms, "ms_fwd_bwd": step_ms, "views_per_s": len(cams) * 1e3 / step_ms,
+            "per_view_loop_ms": loop_ms, "speedup_vs_per_view_loop": loop_ms / step_ms,
+            "peak_hbm_gb": peak_gb, "hbm_before_gb": (total - free0) / 1e9,
+            "form": "torch.autograd.Function over gs_train_forward_batched / gs_train_backward_batched "
+                    "(one render lane per view; per-tile recomputation in the blend backward, per-pixel state "
+                    "= final transmittance + blended count)"}
 
 
 def differentiation_form(dev, quick: bool = False):
@@ -238,12 +323,7 @@ def differentiation_form(dev, quick: bool = False):
     cam = Camera.from_spec(specs[0])
     raw = tp.from_rows(rows)
     params = {k: torch.tensor(v, device=dev, requires_grad=True) for k, v in raw.items()}
-    rng = np.random.default_rng(4)
-    pert = dict(raw)
-    pert["means"] = raw["means"] + rng.normal(0.0, 0.01, raw["means"].shape).astype(np.float32)
-    sh = raw["sh"].reshape(-1, 3, 16).copy()
-    sh[:, :, 0] += rng.normal(0.0, 0.05, sh[:, :, 0].shape).astype(np.float32)
-    pert["sh"] = sh.reshape(-1, 48)
+    pert = _perturbed(raw)
     r = Renderer(rows.shape[0], cam.width, cam.height)
     with torch.no_grad():
         target = train.render({k: torch.tensor(v, device=dev) for k, v in pert.items()}, cam, r).clone()
@@ -485,7 +565,7 @@ def run_ours(args):
                      "unit": "T lane-ops/s", "frac": achieved / fp32_peak, "traffic": profile_traffic(),
                      "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
                      "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair met front to "
-                             "back while the pixel's transmittance is >= 2^-24"},
+                             "back while the pixel's transmittance is >= the transmittance floor (1e-4)"},
         "roofline_hbm": {**hbm_stages, "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "stages_ms": stage_mean,
         "dominant_stage": dominant,
@@ -503,6 +583,7 @@ def run_ours(args):
     if not args.no_forms:
         line["batched"] = batched_form(dev, quick=args.steps < 9)
         line["differentiation"] = differentiation_form(dev, quick=args.steps < 9)
+        line["batched_differentiation"] = batched_differentiation_form(dev, quick=args.steps < 9)
     # cull_project, depth sort (histogram + 4 passes), then per depth slab: count, giant count, scan,
     # emit, giant emit, per-tile sort, raster
     launches_per_frame = 1 + 5 + 7 * DEFAULT_SLABS

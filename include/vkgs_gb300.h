@@ -270,6 +270,18 @@ gs_status gs_viewer_create(gs_viewer** viewer, gs_context* context, const gs_spl
 gs_status gs_viewer_frame(gs_viewer* viewer, const gs_camera* camera, gs_stream stream);
 void gs_viewer_destroy(gs_viewer* viewer);
 
+/* The differentiable path over many views of the same splats (no counterpart in the reference): view v
+ * is drawn by render lane v (gs_context_set_batch_lanes; n_views may not exceed the lanes,
+ * GS_ERROR_CAPACITY otherwise), which keeps that view's forward state; the activation runs once.  The
+ * backward runs every view's blend and projection backward concurrently and adds all views' gradients
+ * into the one set of buffers (atomically), as a loss summed over the views requires.  Both calls are
+ * ordered on `stream` (fork/join over the lanes' streams). */
+gs_status gs_train_forward_batched(gs_context* context, const gs_train_params* params, uint32_t n_views,
+                                   const gs_camera* cameras, float* const* colors_rgba32f, gs_stream stream);
+gs_status gs_train_backward_batched(gs_context* context, const gs_train_params* params, uint32_t n_views,
+                                    const gs_camera* cameras, const float* const* grads_rgba32f,
+                                    const gs_train_grads* grads, gs_stream stream);
+
 /* Per-stage GPU timing, the counterpart of the reference's timestamp queries (engine.cc:471-478,
  * 1033-1045).  While enabled, gs_render records CUDA events on its stream around each stage; the
  * events of the last 256 frames are kept.  Stages, in order: cull + key + projection, depth sort,

@@ -86,3 +86,65 @@ def test_train_rejects_bad_shapes(cuda):
     cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=64, height=64))
     with pytest.raises(ValueError):
         train.render(p, cam, r)
+
+
+def test_batched_gradients_equal_sum_of_views(cuda, oracle):
+    """The batched differentiable path draws each view exactly as the one-view path and its gradients are
+    the per-view gradients summed (atomic accumulation: equal up to FP32 summation order)."""
+    import torch
+    from vkgs_gb300 import Renderer, train
+
+    n = 20_000
+    rows = syn.splat_rows(n, 11)
+    eyes = [(0.0, 0.0, 6.0), (1.5, 0.5, 4.0), (-2.0, 1.0, 5.0), (0.5, -1.5, 4.5), (3.0, 0.0, 3.0)]
+    sizes = [(160, 120), (128, 128), (200, 90), (96, 160), (144, 144)]
+    cams = [scenes.product_camera(scenes.camera(oracle, e, width=w, height=h)) for e, (w, h) in zip(eyes, sizes)]
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    weights = [torch.randn((h, w, 4), device="cuda", generator=gen) for (w, h) in sizes]
+
+    ref = {k: torch.zeros_like(v) for k, v in _gpu_params(rows).items()}
+    single = Renderer(n, 200, 160)
+    imgs1 = []
+    for cam, wt in zip(cams, weights):
+        p = _gpu_params(rows)
+        img = train.render(p, cam, single)
+        (img * wt).sum().backward()
+        imgs1.append(img.detach())
+        for k in train.NAMES:
+            ref[k] += p[k].grad
+
+    r = Renderer(n, 200, 160)
+    r.set_batch_lanes(len(cams))
+    params = _gpu_params(rows)
+    imgs = train.render_batched(params, cams, r)
+    sum((img * wt).sum() for img, wt in zip(imgs, weights)).backward()
+    r.check()
+    for img, img1 in zip(imgs, imgs1):
+        assert torch.equal(img.detach(), img1)
+    for k in train.NAMES:
+        g, g1 = params[k].grad, ref[k]
+        rel = float((g - g1).norm() / g1.norm())
+        assert rel <= 1e-5, (k, rel)
+
+
+def test_batched_train_needs_a_lane_per_view(cuda):
+    import ctypes
+
+    import torch
+    from vkgs_gb300 import Camera, Renderer, _lib as L, train
+
+    r = Renderer(10, 64, 64)
+    p = {k: torch.zeros((10,) + train.SHAPES[k], device="cuda") for k in train.NAMES}
+    p["quats"][:, 3] = 1.0
+    cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=64, height=64))
+    r.set_batch_lanes(2)
+    tensors = [p[k] for k in train.NAMES]
+    imgs = [torch.empty((64, 64, 4), device="cuda") for _ in range(3)]
+    tp_ = train._train_params(tensors)
+    cams = (L.GsCamera * 3)(*[cam.struct()] * 3)
+    ptrs = (ctypes.c_void_p * 3)(*[im.data_ptr() for im in imgs])
+    st = r._lib.gs_train_forward_batched(r._h, ctypes.byref(tp_), 3, cams, ptrs, None)
+    assert st == L.GS_ERROR_CAPACITY
+    imgs = train.forward_batched(r, tensors, [cam] * 3)  # the Python side adds lanes
+    assert r.batch_lanes == 3 and len(imgs) == 3
+    r.check()

@@ -98,6 +98,11 @@ SIGNATURES = [
     ("gs_train_forward", c_int, [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, c_void_p]),
     ("gs_train_backward", c_int,
      [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, POINTER(GsTrainGrads), c_void_p]),
+    ("gs_train_forward_batched", c_int,
+     [c_void_p, POINTER(GsTrainParams), c_uint32, POINTER(GsCamera), POINTER(c_void_p), c_void_p]),
+    ("gs_train_backward_batched", c_int,
+     [c_void_p, POINTER(GsTrainParams), c_uint32, POINTER(GsCamera), POINTER(c_void_p), POINTER(GsTrainGrads),
+      c_void_p]),
     ("gs_context_enable_timing", c_int, [c_void_p, c_int]),
     ("gs_context_stage_times", c_int, [c_void_p, c_uint32, POINTER(c_float), POINTER(c_uint32)]),
     ("gs_ply_offsets_from_header", c_int,

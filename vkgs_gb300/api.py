@@ -241,6 +241,11 @@ class Renderer:
     def set_batch_lanes(self, lanes: int) -> None:
         """Render lanes for render_batched (sub-contexts with their own scratch and stream; 0 = none)."""
         _check(self._lib.gs_context_set_batch_lanes(self._h, int(lanes)), "gs_context_set_batch_lanes")
+        self._lanes = int(lanes)
+
+    @property
+    def batch_lanes(self) -> int:
+        return getattr(self, "_lanes", 0)
 
     def render_batched(self, splats: Splats, cameras, colors, stream=None):
         """Renders every camera into its own RGBA float32 target (H_v, W_v, 4) in one call (gs_render_batched)."""

@@ -689,16 +689,18 @@ gs_status gs_train_forward(gs_context* c, const gs_train_params* p, const gs_cam
   return render_frame(c, &s, p->sh, cam, &t, nullptr, stream);
 }
 
-gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
-                            const gs_train_grads* g, gs_stream stream) {
-  if (!c || !grad_rgba || !g) return GS_ERROR_INVALID_ARGUMENT;
-  const gs_status v = check_train_params(c, p, cam);
-  if (v != GS_SUCCESS) return v;
+static gs_status check_train_grads(const gs_train_params* p, const gs_train_grads* g) {
+  if (!g) return GS_ERROR_INVALID_ARGUMENT;
   if (p->count && (!g->means || !g->log_scales || !g->quats || !g->opacity_logits || !g->sh))
     return GS_ERROR_INVALID_ARGUMENT;
   if (((reinterpret_cast<uintptr_t>(g->quats) | reinterpret_cast<uintptr_t>(g->sh)) & 15u) != 0)
     return GS_ERROR_INVALID_ARGUMENT;
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  return GS_SUCCESS;
+}
+
+// The backward of the last differentiable forward held by context c (one view).
+static gs_status train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
+                                const gs_train_grads* g, bool atomic, cudaStream_t st) {
   const u32 W = cam->width, H = cam->height;
   if (cudaMemsetAsync(c->grad_rec, 0, (size_t)p->count * kGradRec * sizeof(float), st) != cudaSuccess)
     return GS_ERROR_CUDA;
@@ -732,7 +734,87 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
   ta.g_quats = g->quats;
   ta.g_opacity_logits = g->opacity_logits;
   ta.g_sh = g->sh;
-  return from_cuda(launch_project_backward(fc, ta, st));
+  return from_cuda(launch_project_backward(fc, ta, atomic, st));
+}
+
+gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
+                            const gs_train_grads* g, gs_stream stream) {
+  if (!c || !grad_rgba) return GS_ERROR_INVALID_ARGUMENT;
+  gs_status v = check_train_params(c, p, cam);
+  if (v == GS_SUCCESS) v = check_train_grads(p, g);
+  if (v != GS_SUCCESS) return v;
+  return train_backward(c, p, cam, grad_rgba, g, false, reinterpret_cast<cudaStream_t>(stream));
+}
+
+// Batched differentiable path: view v is drawn by render lane v, which keeps that view's forward state
+// for the backward; the lanes' projection backwards add into the shared gradients atomically.
+static gs_status fork_lanes(gs_context* c, u32 used, cudaStream_t st) {
+  if (cudaEventRecord(c->batch_fork, st) != cudaSuccess) return GS_ERROR_CUDA;
+  for (u32 l = 0; l < used; ++l)
+    if (cudaStreamWaitEvent(c->lane_stream[l], c->batch_fork, 0) != cudaSuccess) return GS_ERROR_CUDA;
+  return GS_SUCCESS;
+}
+
+static gs_status join_lanes(gs_context* c, u32 used, cudaStream_t st) {
+  for (u32 l = 0; l < used; ++l) {
+    if (cudaEventRecord(c->lane_join[l], c->lane_stream[l]) != cudaSuccess) return GS_ERROR_CUDA;
+    if (cudaStreamWaitEvent(st, c->lane_join[l], 0) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  return GS_SUCCESS;
+}
+
+gs_status gs_train_forward_batched(gs_context* c, const gs_train_params* p, uint32_t n_views, const gs_camera* cams,
+                                   float* const* colors, gs_stream stream) {
+  if (!c || (n_views && (!cams || !colors))) return GS_ERROR_INVALID_ARGUMENT;
+  if (n_views > c->nlanes) return GS_ERROR_CAPACITY;  // one lane per view holds its forward state
+  for (u32 v = 0; v < n_views; ++v) {
+    const gs_status r = check_train_params(c, p, &cams[v]);
+    if (r != GS_SUCCESS) return r;
+    if (!colors[v]) return GS_ERROR_INVALID_ARGUMENT;
+  }
+  if (n_views == 0) return GS_SUCCESS;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  TrainArgs ta{};  // the activation once, shared by every view
+  ta.means = p->means;
+  ta.log_scales = p->log_scales;
+  ta.quats = p->quats;
+  ta.opacity_logits = p->opacity_logits;
+  ta.sh = p->sh;
+  ta.n = p->count;
+  ta.position = c->train_pos;
+  ta.cov3d = c->train_cov;
+  ta.opacity = c->train_opacity;
+  if (launch_activate(ta, st) != cudaSuccess) return GS_ERROR_CUDA;
+  gs_status r = fork_lanes(c, n_views, st);
+  if (r != GS_SUCCESS) return r;
+  const gs_splats s{c->train_pos, c->train_cov, c->train_opacity, nullptr, p->count};
+  for (u32 v = 0; v < n_views; ++v) {
+    gs_target t{colors[v], nullptr, nullptr};
+    r = render_frame(c->lane[v], &s, p->sh, &cams[v], &t, nullptr, reinterpret_cast<gs_stream>(c->lane_stream[v]));
+    if (r != GS_SUCCESS) return r;
+  }
+  c->last_batched = true;
+  return join_lanes(c, n_views, st);
+}
+
+gs_status gs_train_backward_batched(gs_context* c, const gs_train_params* p, uint32_t n_views, const gs_camera* cams,
+                                    const float* const* grads_rgba, const gs_train_grads* g, gs_stream stream) {
+  if (!c || (n_views && (!cams || !grads_rgba))) return GS_ERROR_INVALID_ARGUMENT;
+  if (n_views > c->nlanes) return GS_ERROR_CAPACITY;
+  for (u32 v = 0; v < n_views; ++v) {
+    const gs_status r = check_train_params(c, p, &cams[v]);
+    if (r != GS_SUCCESS) return r;
+    if (!grads_rgba[v]) return GS_ERROR_INVALID_ARGUMENT;
+  }
+  gs_status r = check_train_grads(p, g);
+  if (r != GS_SUCCESS || n_views == 0) return r;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if ((r = fork_lanes(c, n_views, st)) != GS_SUCCESS) return r;
+  for (u32 v = 0; v < n_views; ++v) {
+    r = train_backward(c->lane[v], p, &cams[v], grads_rgba[v], g, true, c->lane_stream[v]);
+    if (r != GS_SUCCESS) return r;
+  }
+  return join_lanes(c, n_views, st);
 }
 
 // ------------------------------------------------------------------ viewer loop (CUDA graph per frame)

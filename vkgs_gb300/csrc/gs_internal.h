@@ -162,7 +162,8 @@ struct TrainArgs {
   float* g_sh;
 };
 cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream);
-cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, cudaStream_t stream);
+// atomic: gradients of several views may be added concurrently (the batched form)
+cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, bool atomic, cudaStream_t stream);
 
 // ---- loader (gs_ply.cu) ----
 struct PlyOffsets {

@@ -79,6 +79,24 @@ __device__ __forceinline__ void sh_basis_grad(float x, float y, float z, float B
 // m (column-major 4x4) as a row-major 3x3 / 4x4 element
 __device__ __forceinline__ float mel(const float* m, int r, int c) { return m[c * 4 + r]; }
 
+// ATOMIC: several views add into the same gradient buffers concurrently (the batched form).
+template <bool ATOMIC>
+__device__ __forceinline__ void add4(float4* p, float4 v) {
+  if (ATOMIC) {
+    atomicAdd(p, v);
+  } else {
+    float4 o = *p;
+    *p = make_float4(o.x + v.x, o.y + v.y, o.z + v.z, o.w + v.w);
+  }
+}
+
+template <bool ATOMIC>
+__device__ __forceinline__ void add1(float* p, float v) {
+  if (ATOMIC) atomicAdd(p, v);
+  else *p += v;
+}
+
+template <bool ATOMIC>
 __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
   const u32 stride = gridDim.x * blockDim.x;
   for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
@@ -190,11 +208,8 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
       const float gc = (col > 0.0f && col < 1.0f) ? gr[6 + ch] : 0.0f;  // max(., 0) and the target's clamp
       if (gc == 0.0f) continue;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        float4 acc = gsh[4 * ch + k];
-        acc.x += B[4 * k] * gc, acc.y += B[4 * k + 1] * gc, acc.z += B[4 * k + 2] * gc, acc.w += B[4 * k + 3] * gc;
-        gsh[4 * ch + k] = acc;
-      }
+      for (int k = 0; k < 4; ++k)
+        add4<ATOMIC>(gsh + 4 * ch + k, make_float4(B[4 * k] * gc, B[4 * k + 1] * gc, B[4 * k + 2] * gc, B[4 * k + 3] * gc));
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
         const float w = c16[k] * gc;
@@ -285,26 +300,25 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
             4.0f * qz * (gR[0][0] + gR[1][1]);
     gq[3] = 2.0f * (qz * (gR[1][0] - gR[0][1]) + qy * (gR[0][2] - gR[2][0]) + qx * (gR[2][1] - gR[1][2]));
     const float qd = qn[0] * gq[0] + qn[1] * gq[1] + qn[2] * gq[2] + qn[3] * gq[3];
-    float4* gq4 = reinterpret_cast<float4*>(a.g_quats) + id;
-    float4 acc = *gq4;
-    acc.x += (gq[0] - qn[0] * qd) / qlen;
-    acc.y += (gq[1] - qn[1] * qd) / qlen;
-    acc.z += (gq[2] - qn[2] * qd) / qlen;
-    acc.w += (gq[3] - qn[3] * qd) / qlen;
-    *gq4 = acc;
+    add4<ATOMIC>(reinterpret_cast<float4*>(a.g_quats) + id,
+                 make_float4((gq[0] - qn[0] * qd) / qlen, (gq[1] - qn[1] * qd) / qlen, (gq[2] - qn[2] * qd) / qlen,
+                             (gq[3] - qn[3] * qd) / qlen));
     (void)qraw;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      a.g_log_scales[3 * id + i] += gsc[i] * sc[i];
-      a.g_means[3 * id + i] += gpos[i];
+      add1<ATOMIC>(a.g_log_scales + 3 * id + i, gsc[i] * sc[i]);
+      add1<ATOMIC>(a.g_means + 3 * id + i, gpos[i]);
     }
-    a.g_opacity_logits[id] += gr[5] * o * (1.0f - o);
+    add1<ATOMIC>(a.g_opacity_logits + id, gr[5] * o * (1.0f - o));
   }
 }
 
-cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, cudaStream_t stream) {
+cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, bool atomic, cudaStream_t stream) {
   if (a.n == 0) return cudaSuccess;
-  k_project_backward<<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(fc, a);
+  if (atomic)
+    k_project_backward<true><<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(fc, a);
+  else
+    k_project_backward<false><<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(fc, a);
   return cudaGetLastError();
 }
 

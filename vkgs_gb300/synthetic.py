@@ -124,10 +124,10 @@ def random_cameras(count: int, seed: int, radius=(6.0, 12.0), fovy=(40.0, 75.0),
 WORKLOADS = {
     "small": dict(n=100_000, seed=0, layout="gaussian"),
     "large": dict(n=6_000_000, seed=1, layout="shell"),
-    "batched": dict(n=1_000_000, seed=2, layout="gaussian"),
+    "batched": dict(n=1_000_000, seed=2, layout="shell"),
     "grad_check": dict(n=1_000, seed=3, layout="gaussian"),
     "grad": dict(n=200_000, seed=3, layout="gaussian"),
-    "batched_grad": dict(n=3_000_000, seed=4, layout="gaussian"),
+    "batched_grad": dict(n=3_000_000, seed=4, layout="shell"),
 }
 
 
