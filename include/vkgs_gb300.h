@@ -214,7 +214,7 @@ gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32
 /* Creates `lanes` render lanes (0 ... GS_MAX_LANES) with this context's capacities, slab schedule and
  * counting mode (later gs_context_reserve / set_slabs / set_count_fragments calls apply to them too).
  * Synchronises the device and allocates: not for use inside a capture. */
-#define GS_MAX_LANES 16
+#define GS_MAX_LANES 32
 gs_status gs_context_set_batch_lanes(gs_context* context, uint32_t lanes);
 
 /* ------------------------------------------------------------------------ */

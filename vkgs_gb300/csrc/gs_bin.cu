@@ -16,9 +16,9 @@
 //              splat's sorted position to its tile's segment through the cursor (atomicAdd): each
 //              segment holds the right set of splats in arbitrary order
 //   4. sort  : one CTA per tile, longest segments first, sorts its segment by sorted position
-//              (comparison ranks for short segments, LSD radix in shared memory over the segment's
-//              key range otherwise) and writes the splat ids; a tile whose cursor did not end exactly
-//              at its segment end fails the self-check.
+//              (comparison ranks for short segments, a one-pass bucket sort over the segment's key
+//              range otherwise: the keys are distinct) and writes the splat ids; a tile whose cursor
+//              did not end exactly at its segment end fails the self-check.
 // The tile test is exact up to a small margin: the quad (corners c +- a +- b) is clipped to each tile
 // row's band of pixel centres and the tile columns its x-extent reaches are taken; the margin only
 // ever adds pairs.  count and emit evaluate the same footprint arithmetic (this unit is compiled
@@ -38,7 +38,10 @@ constexpr u32 kGiantThreads = 256;
 constexpr u32 kGiantRows = 1024;    // row prefix held in shared memory per window
 constexpr u32 kSortThreads = 256;
 constexpr u32 kSortWarps = kSortThreads / 32;
-constexpr u32 kSortChunk = 3072;    // keys ranked per shared-memory round
+constexpr u32 kSortChunk = 3072;    // segments up to this length are sorted in shared memory
+constexpr u32 kSortItems = kSortChunk / kSortThreads;
+constexpr u32 kSortSmall = 64;      // segments up to this length are ranked by direct comparison
+constexpr u32 kSortLogBuckets = 12;
 
 // The quad of one splat prepared for row clipping: corners in order and inverse edge slopes.
 struct Footprint {
@@ -494,80 +497,40 @@ __global__ __launch_bounds__(kGiantThreads) void k_bin_giant_emit(const BinArgs 
   }
 }
 
-// Stable ranking of keys[0..cnt) (shared memory) on digit ((key - kmin) >> shift) & 0xff.  Warp w owns
-// elements [w * 32 * ipw, (w + 1) * 32 * ipw), item i of a lane is element w * 32 * ipw + i * 32 + lane.
-// Leaves s_rank[e] = rank among the warp's earlier elements of the same digit, s_whist[w][d] = the
-// elements of digit d in warps before w, s_dcount[d] = the digit's total.  Whole CTA.
-__device__ __forceinline__ void rank_chunk(const u32* keys, u32 cnt, u32 shift, u32 kmin, unsigned short* s_rank,
-                                           u32 (*s_whist)[256], u32* s_dcount) {
-  const u32 tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-  for (u32 i = tid; i < kSortWarps * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
-  __syncthreads();
-  const u32 ipw = (cnt + kSortThreads - 1) / kSortThreads;
-  const u32 wbase = warp * 32 * ipw;
-  const u32 lt = lanemask_lt();
-  for (u32 i = 0; i < ipw; ++i) {
-    const u32 e = wbase + i * 32 + lane;
-    const bool valid = e < cnt;
-    const u32 d = valid ? ((keys[e] - kmin) >> shift) & 0xffu : 0u;
-    const u32 peers = match_digit8(d, valid);
-    const int leader = valid ? __ffs(peers) - 1 : 0;
-    u32 old = 0;
-    if (valid && (int)lane == leader) old = atomicAdd(&s_whist[warp][d], (u32)__popc(peers));
-    old = __shfl_sync(0xffffffffu, old, leader);
-    if (valid) s_rank[e] = (unsigned short)(old + __popc(peers & lt));
+// Bucket layout of one segment's keys (distinct sorted positions): bucket(k) = (k - kmin) >> shift,
+// about two buckets per key (at most 2^kSortLogBuckets), so that buckets hold very few keys.
+struct Buckets {
+  u32 kmin, shift, nbk;
+  __device__ __forceinline__ u32 of(u32 k) const { return (k - kmin) >> shift; }
+};
+
+__device__ __forceinline__ Buckets make_buckets(u32 kmin, u32 kmax, u32 n) {
+  const u32 bits = 32 - __clz(kmax - kmin);                   // bits of the key range
+  const u32 lb = min(kSortLogBuckets, 33 - __clz(n - 1));     // ceil(log2 n) + 1, n >= 2
+  const u32 shift = bits > lb ? bits - lb : 0;
+  return Buckets{kmin, shift, ((kmax - kmin) >> shift) + 1};  // <= 2^lb buckets
+}
+
+// In place: s_cnt[0..nbk) counts -> exclusive starts, s_cnt[nbk] = total.  Whole CTA.
+__device__ __forceinline__ void scan_buckets(u32* s_cnt, u32 nbk, u32* s_scan) {
+  const u32 per = (nbk + kSortThreads - 1) / kSortThreads;
+  const u32 b0 = min(threadIdx.x * per, nbk), b1 = min(b0 + per, nbk);
+  u32 s = 0;
+  for (u32 b = b0; b < b1; ++b) s += s_cnt[b];
+  u32 total;
+  u32 run = block_exclusive_scan<kSortThreads>(s, s_scan, &total);
+  for (u32 b = b0; b < b1; ++b) {
+    const u32 c = s_cnt[b];
+    s_cnt[b] = run;
+    run += c;
   }
-  __syncthreads();
-  u32 acc = 0;
-#pragma unroll
-  for (u32 w = 0; w < kSortWarps; ++w) {
-    const u32 c = s_whist[w][tid];
-    s_whist[w][tid] = acc;
-    acc += c;
-  }
-  s_dcount[tid] = acc;
+  if (threadIdx.x == 0) s_cnt[nbk] = total;
   __syncthreads();
 }
 
-// 4. one CTA per tile (longest segments first): sort the segment's sorted positions ascending and
-//    write the splat ids in that order.  Up to kSortThreads keys: rank by comparison; up to
-//    kSortChunk: LSD radix in shared memory over the segment's key range; longer: the same passes
-//    streaming the segment through shared memory in chunks.
-__global__ __launch_bounds__(kSortThreads) void k_tile_sort(const BinArgs a) {
-  __shared__ u32 s_keys[2][kSortChunk];
-  __shared__ unsigned short s_rank[kSortChunk];
-  __shared__ u32 s_whist[kSortWarps][256];
-  __shared__ u32 s_dcount[256];
-  __shared__ u32 s_dpos[256];
-  __shared__ u32 s_scan[32];
-  __shared__ u32 s_red[2][kSortWarps];
-  const u32 t = a.tile_order[blockIdx.x], tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-  if (a.tile_done && tile_is_done(a.tile_done, t)) return;
-  const u32 start = a.tile_range[2 * t], cursor = a.tile_range[2 * t + 1], end = a.tile_range[2 * t + 2];
-  if (tid == 0 && cursor != end) atomicOr(a.err, ERR_INTERNAL);  // emitted pairs != counted pairs
-  const u32 x = min(start, a.pair_capacity), n = min(cursor, a.pair_capacity) - x;
-  if (n == 0) return;
-  u32* key = a.pair_key + x;
-  u32* out = a.pair_splat + x;
-  if (n <= kSortThreads) {  // a key's rank by direct comparison with all the others (keys are distinct)
-    const u32 k = tid < n ? key[tid] : 0u;
-    s_keys[0][tid] = k;
-    __syncthreads();
-    if (tid < n) {
-      u32 rank = 0;
-      for (u32 j = 0; j < n; ++j) rank += s_keys[0][j] < k ? 1u : 0u;
-      out[rank] = __ldg(a.index + k);
-    }
-    return;
-  }
-  // key range of the segment: the radix passes cover only its bits
-  u32 kmin = 0xffffffffu, kmax = 0;
-  for (u32 e = tid; e < n; e += kSortThreads) {
-    const u32 k = key[e];
-    kmin = min(kmin, k);
-    kmax = max(kmax, k);
-    if (n <= kSortChunk) s_keys[0][e] = k;
-  }
+// Minimum and maximum over the CTA (thread values in, block values out).  Whole CTA.
+__device__ __forceinline__ void block_min_max(u32& kmin, u32& kmax, u32 (*s_red)[kSortWarps]) {
+  const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   kmin = __reduce_min_sync(0xffffffffu, kmin);
   kmax = __reduce_max_sync(0xffffffffu, kmax);
   if (lane == 0) {
@@ -582,67 +545,107 @@ __global__ __launch_bounds__(kSortThreads) void k_tile_sort(const BinArgs a) {
     kmin = min(kmin, s_red[0][w]);
     kmax = max(kmax, s_red[1][w]);
   }
-  const u32 bits = 32 - __clz(kmax - kmin);
-  const u32 passes = (bits + 7) / 8;
-  if (n <= kSortChunk) {  // the whole segment stays in shared memory
-    const u32 ipw = (n + kSortThreads - 1) / kSortThreads;
-    u32 cur = 0;
-    for (u32 p = 0; p < passes; ++p) {
-      const u32 shift = 8 * p;
-      rank_chunk(s_keys[cur], n, shift, kmin, s_rank, s_whist, s_dcount);
-      u32 tot;
-      s_dpos[tid] = block_exclusive_scan<kSortThreads>(s_dcount[tid], s_scan, &tot);
-      __syncthreads();
-      for (u32 i = 0; i < ipw; ++i) {
-        const u32 e = warp * 32 * ipw + i * 32 + lane;
-        if (e < n) {
-          const u32 k = s_keys[cur][e];
-          const u32 d = ((k - kmin) >> shift) & 0xffu;
-          s_keys[cur ^ 1][s_dpos[d] + s_whist[warp][d] + s_rank[e]] = k;
-        }
-      }
-      __syncthreads();
-      cur ^= 1;
+}
+
+// 4. one CTA per tile (longest segments first): sort the segment's sorted positions ascending and
+//    write the splat ids in that order.  The keys of a segment are distinct, so a one-pass bucket
+//    sort needs no stability: keys are counted into about 2n buckets over the segment's key range,
+//    scattered to their bucket (any order inside it), and each key's final place is its bucket's
+//    start plus the keys of its bucket below it.  Up to kSortSmall keys: rank by direct comparison;
+//    up to kSortChunk: everything in shared memory; longer: the same steps through the segment's
+//    key and output arrays in global memory.
+__global__ __launch_bounds__(kSortThreads) void k_tile_sort(const BinArgs a) {
+  __shared__ u32 s_cnt[(1u << kSortLogBuckets) + 1];
+  __shared__ u32 s_a[kSortChunk];
+  __shared__ u32 s_b[kSortChunk];
+  __shared__ u32 s_scan[32];
+  __shared__ u32 s_red[2][kSortWarps];
+  const u32 t = a.tile_order[blockIdx.x], tid = threadIdx.x;
+  if (a.tile_done && tile_is_done(a.tile_done, t)) return;
+  const u32 start = a.tile_range[2 * t], cursor = a.tile_range[2 * t + 1], end = a.tile_range[2 * t + 2];
+  if (tid == 0 && cursor != end) atomicOr(a.err, ERR_INTERNAL);  // emitted pairs != counted pairs
+  const u32 x = min(start, a.pair_capacity), n = min(cursor, a.pair_capacity) - x;
+  if (n == 0) return;
+  u32* key = a.pair_key + x;
+  u32* out = a.pair_splat + x;
+  if (n <= kSortSmall) {  // a key's rank by direct comparison with all the others
+    const u32 k = tid < n ? key[tid] : 0u;
+    if (tid < n) s_a[tid] = k;
+    __syncthreads();
+    if (tid < n) {
+      u32 rank = 0;
+      for (u32 j = 0; j < n; ++j) rank += s_a[j] < k ? 1u : 0u;
+      out[rank] = __ldg(a.index + k);
     }
-    for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + s_keys[cur][e]);
     return;
   }
-  // Longer segments: each pass streams the segment through shared memory in chunks, in order, with
-  // running digit offsets; the passes alternate between the key and the output array.
-  u32* src = key;
-  u32* dst = out;
-  for (u32 p = 0; p < passes; ++p) {
-    const u32 shift = 8 * p;
-    s_dcount[tid] = 0;
-    __syncthreads();
-    for (u32 e = tid; e < n; e += kSortThreads) atomicAdd(&s_dcount[((src[e] - kmin) >> shift) & 0xffu], 1u);
-    __syncthreads();
-    u32 tot;
-    s_dpos[tid] = block_exclusive_scan<kSortThreads>(s_dcount[tid], s_scan, &tot);
-    __syncthreads();
-    for (u32 base = 0; base < n; base += kSortChunk) {
-      const u32 cnt = min(kSortChunk, n - base);
-      for (u32 e = tid; e < cnt; e += kSortThreads) s_keys[0][e] = src[base + e];
-      __syncthreads();
-      rank_chunk(s_keys[0], cnt, shift, kmin, s_rank, s_whist, s_dcount);
-      const u32 cw = (cnt + kSortThreads - 1) / kSortThreads;
-      for (u32 i = 0; i < cw; ++i) {
-        const u32 e = warp * 32 * cw + i * 32 + lane;
-        if (e < cnt) {
-          const u32 k = s_keys[0][e];
-          const u32 d = ((k - kmin) >> shift) & 0xffu;
-          dst[s_dpos[d] + s_whist[warp][d] + s_rank[e]] = k;
-        }
+  if (n <= kSortChunk) {
+    u32 k[kSortItems], slot[kSortItems];
+    u32 kmin = 0xffffffffu, kmax = 0;
+#pragma unroll
+    for (u32 i = 0; i < kSortItems; ++i) {
+      const u32 e = tid + i * kSortThreads;
+      k[i] = e < n ? key[e] : 0u;
+      if (e < n) {
+        kmin = min(kmin, k[i]);
+        kmax = max(kmax, k[i]);
       }
-      __syncthreads();
-      s_dpos[tid] += s_dcount[tid];
-      __syncthreads();
     }
-    u32* tmp = src;
-    src = dst;
-    dst = tmp;
+    block_min_max(kmin, kmax, s_red);
+    const Buckets bk = make_buckets(kmin, kmax, n);
+    for (u32 b = tid; b <= bk.nbk; b += kSortThreads) s_cnt[b] = 0;
+    __syncthreads();
+#pragma unroll
+    for (u32 i = 0; i < kSortItems; ++i)
+      if (tid + i * kSortThreads < n) slot[i] = atomicAdd(&s_cnt[bk.of(k[i])], 1u);
+    __syncthreads();
+    scan_buckets(s_cnt, bk.nbk, s_scan);
+#pragma unroll
+    for (u32 i = 0; i < kSortItems; ++i)
+      if (tid + i * kSortThreads < n) s_a[s_cnt[bk.of(k[i])] + slot[i]] = k[i];
+    __syncthreads();
+#pragma unroll
+    for (u32 i = 0; i < kSortItems; ++i) {
+      if (tid + i * kSortThreads < n) {
+        const u32 b = bk.of(k[i]), lo = s_cnt[b], hi = s_cnt[b + 1];
+        u32 rank = lo;
+        for (u32 j = lo; j < hi; ++j) rank += s_a[j] < k[i] ? 1u : 0u;
+        s_b[rank] = k[i];
+      }
+    }
+    __syncthreads();
+    for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + s_b[e]);
+    return;
   }
-  for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + src[e]);  // in place when src == out
+  // Longer segments: count, scatter through per-bucket cursors into the output array (after which
+  // s_cnt[b] is bucket b's end and bucket b starts at s_cnt[b - 1]), place each key into the key
+  // array, then gather the splat ids.
+  u32 kmin = 0xffffffffu, kmax = 0;
+  for (u32 e = tid; e < n; e += kSortThreads) {
+    const u32 k = key[e];
+    kmin = min(kmin, k);
+    kmax = max(kmax, k);
+  }
+  block_min_max(kmin, kmax, s_red);
+  const Buckets bk = make_buckets(kmin, kmax, n);
+  for (u32 b = tid; b <= bk.nbk; b += kSortThreads) s_cnt[b] = 0;
+  __syncthreads();
+  for (u32 e = tid; e < n; e += kSortThreads) atomicAdd(&s_cnt[bk.of(key[e])], 1u);
+  __syncthreads();
+  scan_buckets(s_cnt, bk.nbk, s_scan);
+  for (u32 e = tid; e < n; e += kSortThreads) {
+    const u32 k = key[e];
+    out[atomicAdd(&s_cnt[bk.of(k)], 1u)] = k;
+  }
+  __syncthreads();
+  for (u32 e = tid; e < n; e += kSortThreads) {
+    const u32 k = out[e], b = bk.of(k), lo = b ? s_cnt[b - 1] : 0u, hi = s_cnt[b];
+    u32 rank = lo;
+    for (u32 j = lo; j < hi; ++j) rank += out[j] < k ? 1u : 0u;
+    key[rank] = k;
+  }
+  __syncthreads();
+  for (u32 e = tid; e < n; e += kSortThreads) out[e] = __ldg(a.index + key[e]);
 }
 
 size_t bin_diff_words(u32 max_tiles_x, u32 max_tiles_y) { return (size_t)(max_tiles_x + 1) * max_tiles_y; }
