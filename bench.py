@@ -54,6 +54,8 @@ def parse_args():
     p.add_argument("--cpu-band-stride", type=int, default=8, help="CPU sample: blend every k-th 16-row band")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-forms", action="store_true", help="skip the batched / differentiation forms")
+    p.add_argument("--only-form", choices=["batched", "differentiation", "batched_differentiation"], default=None,
+                   help="run just this form and print its JSON (profiling; no headline line)")
     return p.parse_args()
 
 
@@ -410,6 +412,11 @@ def run_ours(args):
     from vkgs_gb300 import Camera, Renderer, parse_ply
     from vkgs_gb300 import _lib as L
 
+    if args.only_form:
+        form = {"batched": batched_form, "differentiation": differentiation_form,
+                "batched_differentiation": batched_differentiation_form}[args.only_form]
+        print(json.dumps({args.only_form: form(dev, quick=args.steps < 9)}), flush=True)
+        return 0
     rows, off, specs, n = make_scene(args.splats)
     rows_t = torch.from_numpy(rows).to(dev)
     host_rows = rows if (rank == 0 and not args.no_cpu_baseline) else None

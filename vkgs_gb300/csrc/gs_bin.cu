@@ -356,11 +356,13 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
 }
 
 constexpr u32 kSpanBuf = 128;  // row spans per warp and window
+constexpr u32 kPairBatch = 4;  // pairs per lane and step of the emission
 
 // Walks the (splat, tile) pairs of 32 consecutive sorted splats (lane = splat; ok = drawn) in sorted
-// order -- splat by splat, row-major inside a splat -- 32 pairs per step, and calls
-// fn(has, tile, owner_lane, j) on every lane of the warp for each step (j = the pair's index among the
-// 32 splats' pairs); returns the number of pairs.  The splats' row spans are listed
+// order -- splat by splat, row-major inside a splat -- 32 * kPairBatch pairs per step, and calls
+// fn(has[], tile[], owner_lane[]) on every lane of the warp for each step (lane l holds pairs
+// j0 + 32 q + l, q < kPairBatch, so that the caller can keep kPairBatch memory operations in flight);
+// returns the number of pairs.  The splats' row spans are listed
 // in shared memory (span = one tile row of one splat) with an exclusive prefix of their widths, so a
 // lane finds the span of pair j by binary search and no lane expands a footprint serially: a splat
 // that covers thousands of tiles costs the whole warp as much as that many small splats.
@@ -417,22 +419,28 @@ __device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const 
     }
     if (lane == 0) s_pfx[m] = pairs;
     __syncwarp();
-    for (u32 j0 = 0; j0 < pairs; j0 += 32) {
-      const u32 j = j0 + lane;
-      const bool has = j < pairs;
-      u32 tile = 0, owner = 0;
-      if (has) {
-        u32 lo = 0, hi = m;  // last span with s_pfx[span] <= j
-        while (hi - lo > 1) {
-          const u32 mid = (lo + hi) >> 1;
-          if (s_pfx[mid] <= j) lo = mid;
-          else hi = mid;
+    for (u32 j0 = 0; j0 < pairs; j0 += 32 * kPairBatch) {
+      bool has[kPairBatch];
+      u32 tile[kPairBatch], owner[kPairBatch];
+#pragma unroll
+      for (u32 q = 0; q < kPairBatch; ++q) {
+        const u32 j = j0 + 32 * q + lane;
+        has[q] = j < pairs;
+        tile[q] = 0;
+        owner[q] = 0;
+        if (has[q]) {
+          u32 lo = 0, hi = m;  // last span with s_pfx[span] <= j
+          while (hi - lo > 1) {
+            const u32 mid = (lo + hi) >> 1;
+            if (s_pfx[mid] <= j) lo = mid;
+            else hi = mid;
+          }
+          const u32 e = s_tile[lo];
+          tile[q] = (e >> 5) + (j - s_pfx[lo]);
+          owner[q] = e & 31u;
         }
-        const u32 e = s_tile[lo];
-        tile = (e >> 5) + (j - s_pfx[lo]);
-        owner = e & 31u;
       }
-      fn(has, tile, owner, done + j);
+      fn(has, tile, owner);
     }
     done += pairs;
     __syncwarp();
@@ -455,11 +463,17 @@ __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
     Footprint f;
     bool ok = false;
     if (c > 0) ok = footprint(a.record, __ldg(a.index + r), g, f);
-    for_each_pair(f, ok, g, s_spans[warp], [&](bool has, u32 tile, u32 owner, u32) {
-      if (has && !(a.tile_done && tile_is_done(a.tile_done, tile))) {
-        const u32 pos = atomicAdd(a.tile_range + 2 * tile + 1, 1u);
-        if (pos < a.pair_capacity) a.pair_key[pos] = r0 + owner;
+    for_each_pair(f, ok, g, s_spans[warp], [&](const bool* has, const u32* tile, const u32* owner) {
+      u32 pos[kPairBatch];
+#pragma unroll
+      for (u32 q = 0; q < kPairBatch; ++q) {  // all slots reserved first: the atomics overlap
+        pos[q] = 0xffffffffu;
+        if (has[q] && !(a.tile_done && tile_is_done(a.tile_done, tile[q])))
+          pos[q] = atomicAdd(a.tile_range + 2 * tile[q] + 1, 1u);
       }
+#pragma unroll
+      for (u32 q = 0; q < kPairBatch; ++q)
+        if (pos[q] < a.pair_capacity) a.pair_key[pos[q]] = r0 + owner[q];
     });
   }
 }
