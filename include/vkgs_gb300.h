@@ -179,7 +179,7 @@ gs_status gs_context_reserve(gs_context* context, const gs_context_options* opti
  * transmittance T falls below t_floor: everything behind it can then move no channel by more than T,
  * so the image differs from the full blend by less than t_floor per channel.  Default 1e-4 (the
  * threshold of the original 3DGS rasteriser; 39x inside a 1/255 tolerance); valid range
- * (0, 1/255].  The differentiable path always uses 2^-24. */
+ * (0, 1/255].  The differentiable path stops at the same floor, exactly per pixel. */
 gs_status gs_context_set_transmittance_floor(gs_context* context, float t_floor);
 
 /* Makes every following gs_render also count fragments (slower; for statistics and tests). */
@@ -245,7 +245,8 @@ typedef struct gs_train_grads {
 /* The frame of gs_render (one depth slab, no caller depth) from raw parameters into an RGBA float
  * target, keeping in the context what gs_train_backward needs: the activated splats, the tile lists,
  * and per pixel its final transmittance and how many list entries it blended (each pixel stops
- * exactly at transmittance 2^-24).  Valid until the context renders again. */
+ * exactly when its transmittance falls below the context's transmittance floor, so the image and the
+ * gradients leave out contributions smaller than the floor).  Valid until the context renders again. */
 gs_status gs_train_forward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
                            float* color_rgba32f, gs_stream stream);
 

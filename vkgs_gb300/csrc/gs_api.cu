@@ -625,7 +625,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     rr.out_rgba = t->color_rgba32f;
     rr.out_bgra = reinterpret_cast<uchar4*>(t->color_bgra8);
     rr.depth = t->depth;
-    rr.t_floor = train ? 5.9604645e-08f : c->t_floor;  // the differentiable path keeps 2^-24
+    rr.t_floor = c->t_floor;
     rr.fragments = c->count_fragments ? reinterpret_cast<unsigned long long*>(c->frame + FW_FRAGMENTS) : nullptr;
     rr.state_c = c->state_c;
     rr.state_t = c->state_t;

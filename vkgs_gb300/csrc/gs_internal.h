@@ -122,14 +122,16 @@ struct RasterArgs {
   float* state_t;            // [H*W] running transmittance between slabs
   u32* tile_done;            // bitmap: tiles finished by an earlier slab (set here when one finishes)
   int first, last;           // first slab: no state to load; last slab: every tile resolves
-  u32* nproc;                // differentiable forward: per pixel, list entries blended (exact 2^-24 stop)
+  u32* nproc;                // differentiable forward: per pixel, list entries blended (exact stop at t_floor)
   unsigned long long* fragments;  // non-null: [0] covered fragments, [1] those met while T >= t_floor
                                   // (disables the early stop)
 };
 cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
 
 // ---- differentiable path (gs_train.cu, gs_raster.cu) ----
-constexpr u32 kGradRec = 12;  // per-splat blend gradients: dcx, dcy, dA, dB, dC (conic xx, yy, xy), do, dr, dg, db
+// per-splat blend gradient record: sums over the splat's pixels of P, P dx, P dy, P dx^2, P dy^2, P dx dy
+// (P = dL/do of the pixel, d = pixel - centre) and dL/d(r, g, b); 3 words of padding
+constexpr u32 kGradRec = 12;
 struct RasterBackwardArgs {
   const u32* tile_range;
   u32 pair_capacity;

@@ -209,7 +209,11 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
 //   dL/dc_i = a_i T_i dL/dRGB,   dL/da_i = T_i (c_i . dL/dRGB + 2 a_i dL/dA) - S / (1 - a_i),
 //   S += (a_i c_i . dL/dRGB + a_i^2 dL/dA) T_i,
 // and a_i = o exp(-q/2), q = d^T K d with K = M^T M the conic (M = rot_scale^-1, d = pixel - centre):
-//   dL/do = dL/da e^{-q/2},  dq/dcentre = -2 K d,  dq/dK = (dx^2, dy^2, 2 dx dy) for (Kxx, Kyy, Kxy).
+//   dL/do = dL/da e^{-q/2} =: P,  dL/dq = -o P / 2,  dq/dcentre = -2 K d,  dq/dK = (dx^2, dy^2, 2 dx dy).
+// K and o are per splat, so a splat's centre and conic gradients follow from the moments of P over its
+// pixels -- sum P, P dx, P dy, P dx^2, P dy^2, P dx dy -- which is what the pixels accumulate (the
+// projection backward turns them into dL/dcentre = o K (sum P d) and dL/dK = -o/2 (sum P dx^2, sum P dy^2,
+// 2 sum P dx dy)).
 // Sums 9 values over the warp by recursive halving: after three halving steps each group of four lanes
 // holds one of v[0..7] (index = lane bits 4, 3, 2), finished by two more shuffles; v[8] is summed
 // alone.  14 shuffles instead of 45.  Lane 4k (k < 8) returns the total of v[k], lane 0 also *v8.
@@ -314,15 +318,14 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
           const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
           S += (al * cg + al * al * g.w) * Ti;
           Tcur = Ti;
-          const float dLdq = -0.5f * al * dLda;
-          const float Kxx = q0.z * q0.z + q1.x * q1.x, Kyy = q0.w * q0.w + q1.y * q1.y;
-          const float Kxy = q0.z * q0.w + q1.x * q1.y;
-          r[0] = -2.0f * dLdq * (Kxx * dx + Kxy * dy);  // d/d centre x
-          r[1] = -2.0f * dLdq * (Kxy * dx + Kyy * dy);  // d/d centre y
-          r[2] = dLdq * dx * dx;                        // d/d Kxx
-          r[3] = dLdq * dy * dy;                        // d/d Kyy
-          r[4] = dLdq * 2.0f * dx * dy;                 // d/d Kxy
-          r[5] = dLda * G;                              // d/d opacity
+          const float P = dLda * G;  // dL/do of this pixel; dL/dq = -o P / 2
+          const float pdx = P * dx, pdy = P * dy;
+          r[0] = P;
+          r[1] = pdx;
+          r[2] = pdy;
+          r[3] = pdx * dx;
+          r[4] = pdy * dy;
+          r[5] = pdx * dy;
           const float w = al * Ti;
           r[6] = w * g.x;
           r[7] = w * g.y;

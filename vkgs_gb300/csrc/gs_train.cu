@@ -179,6 +179,10 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
     const float sa = S2[0][0], sb = S2[1][1], scc = 0.5f * (S2[0][1] + S2[1][0]);
     const float det = sa * sb - scc * scc;
     const float K[2][2] = {{sb / det, -scc / det}, {-scc / det, sa / det}};
+    // the blend's moments -> centre and conic gradients (K and o are constant over the splat's pixels)
+    const float g_cx = o * (K[0][0] * gr[1] + K[0][1] * gr[2]), g_cy = o * (K[1][0] * gr[1] + K[1][1] * gr[2]);
+    const float g_kxx = -0.5f * o * gr[3], g_kyy = -0.5f * o * gr[4], g_kxy2 = -o * gr[5];  // Kxy counted twice
+    const float g_o = gr[0];
     float pc[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -220,7 +224,7 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
     float gpos[3] = {(gdir[0] - dir[0] * dd) / dl, (gdir[1] - dir[1] * dd) / dl, (gdir[2] - dir[2] * dd) / dl};
 
     // ---- conic -> cov2d -> C2 -> (J, Cv) -> cov3d
-    const float Gb[2][2] = {{gr[2], 0.5f * gr[4]}, {0.5f * gr[4], gr[3]}};
+    const float Gb[2][2] = {{g_kxx, 0.5f * g_kxy2}, {0.5f * g_kxy2, g_kyy}};
     float KG[2][2], gS2[2][2];
 #pragma unroll
     for (int r = 0; r < 2; ++r)
@@ -259,7 +263,7 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
                     (gJ[0][0] + gJ[1][1]) * iz2 - 2.0f * (x * gJ[0][2] + y * gJ[1][2]) * iz3};
     // centre: (P pv).xy / w
     const float iw = 1.0f / pc[3];
-    const float gpc[4] = {gr[0] * iw, gr[1] * iw, 0.0f, -(gr[0] * nx + gr[1] * ny) * iw};
+    const float gpc[4] = {g_cx * iw, g_cy * iw, 0.0f, -(g_cx * nx + g_cy * ny) * iw};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
       gpv[c] += mel(fc.proj, 0, c) * gpc[0] + mel(fc.proj, 1, c) * gpc[1] + mel(fc.proj, 2, c) * gpc[2] +
@@ -309,7 +313,7 @@ __global__ void k_project_backward(const FrameConst fc, const TrainArgs a) {
       add1<ATOMIC>(a.g_log_scales + 3 * id + i, gsc[i] * sc[i]);
       add1<ATOMIC>(a.g_means + 3 * id + i, gpos[i]);
     }
-    add1<ATOMIC>(a.g_opacity_logits + id, gr[5] * o * (1.0f - o));
+    add1<ATOMIC>(a.g_opacity_logits + id, g_o * o * (1.0f - o));
   }
 }
 
