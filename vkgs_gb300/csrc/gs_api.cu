@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -699,8 +700,9 @@ static gs_status check_train_grads(const gs_train_params* p, const gs_train_grad
 }
 
 // The backward of the last differentiable forward held by context c (one view).
-static gs_status train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
-                                const gs_train_grads* g, bool atomic, cudaStream_t st) {
+// The blend backward of the last differentiable forward held by context c: fills c->grad_rec.
+static gs_status blend_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
+                                cudaStream_t st) {
   const u32 W = cam->width, H = cam->height;
   if (cudaMemsetAsync(c->grad_rec, 0, (size_t)p->count * kGradRec * sizeof(float), st) != cudaSuccess)
     return GS_ERROR_CUDA;
@@ -717,9 +719,22 @@ static gs_status train_backward(gs_context* c, const gs_train_params* p, const g
   rb.nproc = c->train_nproc;
   rb.grad_rgba = reinterpret_cast<const float4*>(grad_rgba);
   rb.grad_rec = c->grad_rec;
-  if (launch_raster_backward(rb, st) != cudaSuccess) return GS_ERROR_CUDA;
-  FrameConst fc;
-  frame_constants(cam->projection, cam->view, cam->model, cam->camera_position, W, H, p->count, &fc);
+  return from_cuda(launch_raster_backward(rb, st));
+}
+
+static_assert(kMaxTrainViews >= GS_MAX_LANES, "one projection backward covers every lane's view");
+
+// The projection backward of n views at once; view v's blend gradients are in ctx[v]->grad_rec.
+static gs_status project_backward(gs_context* const* ctx, const gs_camera* cams, u32 n, const gs_train_params* p,
+                                  const gs_train_grads* g, cudaStream_t st) {
+  std::unique_ptr<TrainViews> tv(new TrainViews{});
+  tv->count = n;
+  for (u32 v = 0; v < n; ++v) {
+    const gs_camera& cam = cams[v];
+    frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, p->count,
+                    &tv->fc[v]);
+    tv->grad_rec[v] = ctx[v]->grad_rec;
+  }
   TrainArgs ta{};
   ta.means = p->means;
   ta.log_scales = p->log_scales;
@@ -727,14 +742,12 @@ static gs_status train_backward(gs_context* c, const gs_train_params* p, const g
   ta.opacity_logits = p->opacity_logits;
   ta.sh = p->sh;
   ta.n = p->count;
-  ta.grad_rec = c->grad_rec;
-  ta.record = c->record;
   ta.g_means = g->means;
   ta.g_log_scales = g->log_scales;
   ta.g_quats = g->quats;
   ta.g_opacity_logits = g->opacity_logits;
   ta.g_sh = g->sh;
-  return from_cuda(launch_project_backward(fc, ta, atomic, st));
+  return from_cuda(launch_project_backward(*tv, ta, st));
 }
 
 gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_camera* cam, const float* grad_rgba,
@@ -743,7 +756,9 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
   gs_status v = check_train_params(c, p, cam);
   if (v == GS_SUCCESS) v = check_train_grads(p, g);
   if (v != GS_SUCCESS) return v;
-  return train_backward(c, p, cam, grad_rgba, g, false, reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if ((v = blend_backward(c, p, cam, grad_rgba, st)) != GS_SUCCESS) return v;
+  return project_backward(&c, cam, 1, p, g, st);
 }
 
 // Batched differentiable path: view v is drawn by render lane v, which keeps that view's forward state
@@ -810,11 +825,12 @@ gs_status gs_train_backward_batched(gs_context* c, const gs_train_params* p, uin
   if (r != GS_SUCCESS || n_views == 0) return r;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if ((r = fork_lanes(c, n_views, st)) != GS_SUCCESS) return r;
-  for (u32 v = 0; v < n_views; ++v) {
-    r = train_backward(c->lane[v], p, &cams[v], grads_rgba[v], g, true, c->lane_stream[v]);
+  for (u32 v = 0; v < n_views; ++v) {  // the views' blend backwards run concurrently
+    r = blend_backward(c->lane[v], p, &cams[v], grads_rgba[v], c->lane_stream[v]);
     if (r != GS_SUCCESS) return r;
   }
-  return join_lanes(c, n_views, st);
+  if ((r = join_lanes(c, n_views, st)) != GS_SUCCESS) return r;
+  return project_backward(c->lane, cams, n_views, p, g, st);  // then one pass over the splats for all views
 }
 
 // ------------------------------------------------------------------ viewer loop (CUDA graph per frame)

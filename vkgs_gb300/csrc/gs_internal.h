@@ -155,8 +155,6 @@ struct TrainArgs {
   float* position;  // activated (forward)
   float* cov3d;
   float* opacity;
-  const float* grad_rec;  // backward input
-  const float4* record;   // drawn flags of this frame's records
   float* g_means;         // backward outputs (added into)
   float* g_log_scales;
   float* g_quats;
@@ -164,8 +162,16 @@ struct TrainArgs {
   float* g_sh;
 };
 cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream);
-// atomic: gradients of several views may be added concurrently (the batched form)
-cudaError_t launch_project_backward(const FrameConst& fc, const TrainArgs& a, bool atomic, cudaStream_t stream);
+
+// The views of one differentiable step: camera constants and blend gradient records (kGradRec per splat).
+constexpr u32 kMaxTrainViews = 32;
+struct TrainViews {
+  u32 count;
+  FrameConst fc[kMaxTrainViews];
+  const float* grad_rec[kMaxTrainViews];
+};
+// Adds the raw-parameter gradients of all views into a.g_* (one kernel: no atomics).
+cudaError_t launch_project_backward(const TrainViews& views, const TrainArgs& a, cudaStream_t stream);
 
 // ---- loader (gs_ply.cu) ----
 struct PlyOffsets {

@@ -239,8 +239,11 @@ __device__ __forceinline__ float warp_sum9(float v[9], float* v8) {
   return t;
 }
 
+constexpr u32 kDirectLanes = 4;  // a record covering at most this many pixels of a warp skips the reduction
+
 // Each warp (an 8x4 pixel block) walks only the records that can touch its block, reduces the 9
-// per-splat values over its 32 pixels (warp_sum9) and adds them with one atomic per value.
+// per-splat values over its 32 pixels (warp_sum9) and adds them with one atomic per value; a record
+// that covers only a few of the warp's pixels is added by those lanes directly.
 __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const RasterBackwardArgs a) {
   __shared__ float4 s_q0[kRasterThreads];
   __shared__ float4 s_q1[kRasterThreads];
@@ -331,15 +334,23 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
           r[7] = w * g.y;
           r[8] = w * g.z;
         }
-        if (__any_sync(0xffffffffu, on)) {
-          float r8;
-          const float sum = warp_sum9(r, &r8);
+        const u32 onmask = __ballot_sync(0xffffffffu, on);
+        if (onmask) {
           float* dst = a.grad_rec + (size_t)s_id[j] * kGradRec;
-          if ((lane & 3u) == 0) {
-            const u32 idx = ((lane >> 4) & 1u) * 4u + ((lane >> 3) & 1u) * 2u + ((lane >> 2) & 1u);
-            atomicAdd(dst + idx, sum);
+          if (__popc(onmask) <= kDirectLanes) {  // few pixels: their own atomics beat a warp reduction
+            if (on) {
+#pragma unroll
+              for (int q = 0; q < 9; ++q) atomicAdd(dst + q, r[q]);
+            }
+          } else {
+            float r8;
+            const float sum = warp_sum9(r, &r8);
+            if ((lane & 3u) == 0) {
+              const u32 idx = ((lane >> 4) & 1u) * 4u + ((lane >> 3) & 1u) * 2u + ((lane >> 2) & 1u);
+              atomicAdd(dst + idx, sum);
+            }
+            if (lane == 0) atomicAdd(dst + 8, r8);
           }
-          if (lane == 0) atomicAdd(dst + 8, r8);
         }
       }
     }
