@@ -202,14 +202,21 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
 
 /* No counterpart in the reference (its viewer renders one camera per frame).  Renders n_views cameras
  * of the same splats, view v into targets[v] (sizes may differ; each within the context's maxima), as
- * gs_render would one by one.  The views are spread over the context's render lanes (see
- * gs_context_set_batch_lanes): sub-contexts with their own scratch and stream, forked from `stream`
- * and joined back into it with events, so the batch is ordered on `stream`, allocates nothing and can
- * be captured in a CUDA graph as a whole.  With no lanes the views render one after another on
+ * gs_render would one by one.  With render lanes (gs_context_set_batch_lanes), one cull + projection
+ * pass over the splats serves up to 32 views at a time (each splat's data is read once for all of
+ * them; per-view outputs identical to gs_render's), then each view's depth sort, binning and raster
+ * run on a lane: sub-contexts with their own scratch and stream, forked from `stream` and joined back
+ * into it with events, so the batch is ordered on `stream` and can be captured in a CUDA graph as a
+ * whole.  The shared pass keeps every view's records (72 bytes per splat and view, at most 64 views
+ * at a time); they are allocated by the first batched call that needs them -- if that call is being
+ * captured, it uses a per-lane cull instead.  With no lanes the views render one after another on
  * `stream`.  gs_context_check afterwards reports every lane's errors and the summed statistics
  * (tile_pairs: the largest). */
 gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32_t n_views,
                             const gs_camera* cameras, const gs_target* targets, gs_stream stream);
+
+/* Batched form: 1 (default) = the shared cull + projection pass above, 0 = each lane culls its views. */
+gs_status gs_context_set_batch_shared_cull(gs_context* context, int enable);
 
 /* Creates `lanes` render lanes (0 ... GS_MAX_LANES) with this context's capacities, slab schedule and
  * counting mode (later gs_context_reserve / set_slabs / set_count_fragments calls apply to them too).

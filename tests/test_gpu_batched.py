@@ -22,17 +22,38 @@ def _setup(n, seed, n_views, cam_seed):
     return rows, splats, specs, cams, colors
 
 
-@pytest.mark.parametrize("lanes", [0, 1, 3, 8])
-def test_batched_equals_single_view_renders(cuda, lanes):
-    """Every view of a batch is bit-identical to rendering that camera alone (same kernels, own scratch)."""
+@pytest.mark.parametrize("lanes,shared", [(0, True), (1, True), (3, True), (8, True), (3, False), (8, False)])
+def test_batched_equals_single_view_renders(cuda, lanes, shared):
+    """Every view of a batch is bit-identical to rendering that camera alone (same arithmetic, own
+    scratch), with the shared multi-view cull pass and with per-lane culls."""
     import torch
     from vkgs_gb300 import Renderer
 
     _, splats, specs, cams, colors = _setup(200_000, 11, 10, 501)
     r = Renderer(200_000, 1920, 1080)
     r.set_batch_lanes(lanes)
+    r.set_batch_shared_cull(shared)
     r.render_batched_checked(splats, cams, colors)
     single = Renderer(200_000, 1920, 1080)
+    for cam, col in zip(cams, colors):
+        img, _ = single.render_checked(splats, cam)
+        assert torch.equal(img, col)
+
+
+def test_batched_many_views_in_groups(cuda):
+    """70 views: two shared cull launches (32 views each) per group of 64, then a second group reusing the
+    per-view buffers -- every view still equals its single render."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer
+
+    _, splats, _, _, _ = _setup(30_000, 15, 1, 505)
+    specs = syn.random_cameras(70, seed=506, resolutions=[(320, 180), (256, 256), (200, 120)])
+    cams = [Camera.from_spec(sp) for sp in specs]
+    colors = [torch.empty((c.height, c.width, 4), dtype=torch.float32, device="cuda") for c in cams]
+    r = Renderer(30_000, 320, 256)
+    r.set_batch_lanes(5)
+    r.render_batched_checked(splats, cams, colors)
+    single = Renderer(30_000, 320, 256)
     for cam, col in zip(cams, colors):
         img, _ = single.render_checked(splats, cam)
         assert torch.equal(img, col)

@@ -90,6 +90,7 @@ SIGNATURES = [
     ("gs_viewer_create", c_int, [POINTER(c_void_p), c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget)]),
     ("gs_viewer_frame", c_int, [c_void_p, POINTER(GsCamera), c_void_p]),
     ("gs_viewer_destroy", None, [c_void_p]),
+    ("gs_context_set_batch_shared_cull", c_int, [c_void_p, c_int]),
     ("gs_render_batched", c_int,
      [c_void_p, POINTER(GsSplats), c_uint32, POINTER(GsCamera), POINTER(GsTarget), c_void_p]),
     ("gs_render", c_int,

@@ -243,6 +243,10 @@ class Renderer:
         _check(self._lib.gs_context_set_batch_lanes(self._h, int(lanes)), "gs_context_set_batch_lanes")
         self._lanes = int(lanes)
 
+    def set_batch_shared_cull(self, enable: bool = True) -> None:
+        """Batched form: one cull + projection pass for all views (default) or one per lane."""
+        _check(self._lib.gs_context_set_batch_shared_cull(self._h, int(bool(enable))), "set_batch_shared_cull")
+
     @property
     def batch_lanes(self) -> int:
         return getattr(self, "_lanes", 0)

@@ -101,6 +101,10 @@ struct gs_context {
   float4* state_c = nullptr;  // running pixel sums between depth slabs
   float* state_t = nullptr;
   // batched rendering: render lanes (sub-contexts with their own scratch and stream)
+  bool multi_view_cull = true;  // batched form: one k_cull_views pass for all views (else per lane)
+  char* batch_arena = nullptr;  // per-view cull outputs of the batched form (see batch_buffers)
+  size_t batch_bytes = 0;
+  u32 batch_views = 0, batch_n = 0;
   gs_context* lane[GS_MAX_LANES] = {};
   cudaStream_t lane_stream[GS_MAX_LANES] = {};
   cudaEvent_t lane_join[GS_MAX_LANES] = {};
@@ -399,9 +403,20 @@ static void destroy_lanes(gs_context* c) {
   c->nlanes = 0;
 }
 
+static void free_batch_buffers(gs_context* c) {
+  if (c->batch_arena) {
+    cudaDeviceSynchronize();
+    cudaFree(c->batch_arena);
+  }
+  c->batch_arena = nullptr;
+  c->batch_bytes = 0;
+  c->batch_views = c->batch_n = 0;
+}
+
 void gs_context_destroy(gs_context* c) {
   if (!c) return;
   destroy_lanes(c);
+  free_batch_buffers(c);
   if (c->arena) {
     cudaDeviceSynchronize();
     cudaFree(c->arena);
@@ -504,10 +519,20 @@ gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
   return GS_SUCCESS;
 }
 
+// A view culled and projected beforehand (k_cull_views): its compacted keys/ids, records, visible count.
+struct PreCulled {
+  u32* key;
+  u32* index;
+  float4* record;
+  u32* visible;
+};
+
 // One frame.  sh32 (the differentiable path): FP32 SH instead of s->sh, one depth slab, and the
-// training raster that stores per-pixel blend counts and final transmittance.
+// training raster that stores per-pixel blend counts and final transmittance.  pre: the cull already
+// ran for this view (the batched form); the frame starts at the depth sort on pre's buffers.
 static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh32, const gs_camera* cam,
-                              const gs_target* t, const gs_frame_outputs* outs, gs_stream stream) {
+                              const gs_target* t, const gs_frame_outputs* outs, gs_stream stream,
+                              const PreCulled* pre = nullptr) {
   const bool train = sh32 != nullptr;
   gs_frame_outputs none{};
   const gs_frame_outputs& o = outs ? *outs : none;
@@ -535,8 +560,11 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   // 2-5: depth sort passes), so a frame captured in a CUDA graph replays correctly.
   GS_TRY(cudaMemsetAsync(c->arena + c->status_bytes_begin, 0, c->status_bytes_end - c->status_bytes_begin, st));
   GS_TRY(cudaMemsetAsync(c->tile_done, 0, (size_t)(tiles + 31) / 32 * sizeof(u32), st));
-  u32* key = o.keys ? o.keys : c->key;
-  u32* index = o.index ? o.index : c->index;
+  u32* key = pre ? pre->key : (o.keys ? o.keys : c->key);
+  u32* index = pre ? pre->index : (o.index ? o.index : c->index);
+  float4* record = pre ? pre->record : c->record;
+  u32* visible = c->frame + FW_VISIBLE;
+  if (pre) GS_TRY(cudaMemcpyAsync(visible, pre->visible, sizeof(u32), cudaMemcpyDeviceToDevice, st));
   const bool want_inst = o.instances != nullptr;
 
   CullArgs ca{};
@@ -547,15 +575,15 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   ca.sh32 = sh32;
   ca.key = key;
   ca.index = index;
-  ca.record = c->record;
+  ca.record = record;
   ca.inst_by_id = want_inst ? c->inst_by_id : nullptr;
-  ca.visible_count = c->frame + FW_VISIBLE;
+  ca.visible_count = visible;
   ca.status = c->cull_status;
   ca.ticket = c->frame + FW_TICKET_CULL;
   ca.epoch = 1;
   ca.err = c->err;
   ca.num_sms = c->num_sms;
-  GS_TRY(launch_cull_project(fc, ca, st));
+  if (!pre) GS_TRY(launch_cull_project(fc, ca, st));
   GS_MARK(1);
 
   if (n > 0) {
@@ -564,7 +592,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     ra.values = index;
     ra.keys_alt = c->key_alt;
     ra.values_alt = c->index_alt;
-    ra.count = c->frame + FW_VISIBLE;
+    ra.count = visible;
     ra.max_count = n;
     ra.begin_bit = 0;
     ra.end_bit = 32;
@@ -577,7 +605,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   }
 
   if (want_inst || o.draw_indirect)
-    GS_TRY(launch_instances(index, c->frame + FW_VISIBLE, c->inst_by_id, n, o.instances, o.draw_indirect, st));
+    GS_TRY(launch_instances(index, visible, c->inst_by_id, n, o.instances, o.draw_indirect, st));
   GS_MARK(2);
 
   // Depth slabs, nearest first (one slab when nothing is visible).
@@ -587,8 +615,8 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     const int e = 3 + 4 * (int)k;
     BinArgs ba{};
     ba.index = index;
-    ba.visible_count = c->frame + FW_VISIBLE;
-    ba.record = c->record;
+    ba.visible_count = visible;
+    ba.record = record;
     ba.n = n;
     ba.slab_e0 = k ? c->slab_end[k - 1] : 0;
     ba.slab_e1 = slabs == 1 ? 1024 : c->slab_end[k];
@@ -618,7 +646,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     rr.tile_range = c->tile_range;
     rr.pair_capacity = c->pair_capacity;
     rr.pair_splat = c->pair_splat;
-    rr.record = c->record;
+    rr.record = record;
     rr.width = W;
     rr.height = H;
     rr.tiles_x = tiles_x;
@@ -639,7 +667,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   }
 
   if (o.visible_count)
-    GS_TRY(cudaMemcpyAsync(o.visible_count, c->frame + FW_VISIBLE, sizeof(u32), cudaMemcpyDeviceToDevice, st));
+    GS_TRY(cudaMemcpyAsync(o.visible_count, visible, sizeof(u32), cudaMemcpyDeviceToDevice, st));
 #undef GS_MARK
 #undef GS_TRY
   return GS_SUCCESS;
@@ -935,6 +963,113 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
   return GS_SUCCESS;
 }
 
+// Per-view cull outputs of the batched form, for up to kMaxBatchViews views of up to max_splats splats:
+// [visible words][tickets][look-back status of every view] (cleared per batch), then per view its
+// compacted keys, ids and records.  Allocated by the first batched call that needs them (never while
+// the stream is being captured: that call takes the per-lane cull instead).
+constexpr u32 kMaxBatchViews = 64;
+
+struct BatchLayout {
+  size_t status_off, head_bytes, status_words, view_stride, key_off, index_off, record_off, total;
+};
+
+static BatchLayout batch_layout(u32 views, u32 n) {
+  BatchLayout b{};
+  const auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  b.status_words = (n + kCullTile - 1) / kCullTile;
+  b.status_off = up((size_t)(kMaxBatchViews + kMaxBatchViews / kMaxCullViews + 1) * sizeof(u32));
+  b.head_bytes = b.status_off + up((size_t)views * b.status_words * sizeof(u64));
+  b.key_off = 0;
+  b.index_off = up((size_t)n * sizeof(u32));
+  b.record_off = b.index_off + up((size_t)n * sizeof(u32));
+  b.view_stride = b.record_off + up((size_t)n * 4 * sizeof(float4));
+  b.total = b.head_bytes + (size_t)views * b.view_stride;
+  return b;
+}
+
+static bool batch_buffers(gs_context* c, u32 views, cudaStream_t st) {
+  if (c->batch_arena && views <= c->batch_views && c->max_splats <= c->batch_n) return true;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return false;
+  free_batch_buffers(c);
+  const BatchLayout b = batch_layout(views, c->max_splats);
+  if (cudaMalloc(&c->batch_arena, b.total) != cudaSuccess) {
+    cudaGetLastError();
+    c->batch_arena = nullptr;
+    return false;
+  }
+  c->batch_bytes = b.total;
+  c->batch_views = views;
+  c->batch_n = c->max_splats;
+  return true;
+}
+
+// Views [v0, v0 + nv) of the batch: their culls in k_cull_views launches on `st`, then their frames
+// from the depth sort on, spread over the lanes.
+static gs_status batched_group(gs_context* c, const gs_splats* s, u32 v0, u32 nv, const gs_camera* cams,
+                               const gs_target* targets, cudaStream_t st) {
+  const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
+  char* base = c->batch_arena;
+  u32* visible = reinterpret_cast<u32*>(base);
+  u32* tickets = visible + kMaxBatchViews;
+  u64* status = reinterpret_cast<u64*>(base + b.status_off);
+  char* views = base + b.head_bytes;
+  if (cudaMemsetAsync(base, 0, b.head_bytes, st) != cudaSuccess) return GS_ERROR_CUDA;
+  std::unique_ptr<CullViewsArgs> ca(new CullViewsArgs{});
+  for (u32 c0 = 0; c0 < nv; c0 += kMaxCullViews) {
+    const u32 cnt = std::min(kMaxCullViews, nv - c0);
+    ca->position = s->position;
+    ca->cov3d = s->cov3d;
+    ca->opacity = s->opacity;
+    ca->sh = s->sh;
+    ca->n = s->count;
+    ca->count = cnt;
+    ca->ticket = tickets + c0 / kMaxCullViews;
+    ca->epoch = 1;
+    ca->err = c->err;
+    ca->num_sms = c->num_sms;
+    for (u32 i = 0; i < cnt; ++i) {
+      const u32 w = c0 + i;  // slot in the arena
+      const gs_camera& cam = cams[v0 + w];
+      frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, s->count,
+                      &ca->fc[i]);
+      char* vb = views + (size_t)w * b.view_stride;
+      ca->view[i] = CullView{reinterpret_cast<u32*>(vb + b.key_off), reinterpret_cast<u32*>(vb + b.index_off),
+                             reinterpret_cast<float4*>(vb + b.record_off), visible + w, status + (size_t)w * b.status_words};
+    }
+    if (launch_cull_views(*ca, st) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  const u32 used = std::min(c->nlanes, std::max(nv, 1u));
+  gs_status r = fork_lanes(c, used, st);
+  if (r != GS_SUCCESS) return r;
+  // Largest views first, each to the lane with the least work so far (work ~ pixels + a fixed cost per
+  // view), so the lanes finish together.
+  std::vector<u32> order(nv);
+  for (u32 w = 0; w < nv; ++w) order[w] = w;
+  const auto work = [&](u32 w) { return (double)cams[v0 + w].width * cams[v0 + w].height + 250000.0; };
+  std::stable_sort(order.begin(), order.end(), [&](u32 x, u32 y) { return work(x) > work(y); });
+  double load[GS_MAX_LANES] = {};
+  for (u32 w : order) {
+    u32 l = 0;
+    for (u32 k = 1; k < used; ++k)
+      if (load[k] < load[l]) l = k;
+    load[l] += work(w);
+    char* vb = views + (size_t)w * b.view_stride;
+    const PreCulled pre{reinterpret_cast<u32*>(vb + b.key_off), reinterpret_cast<u32*>(vb + b.index_off),
+                        reinterpret_cast<float4*>(vb + b.record_off), visible + w};
+    r = render_frame(c->lane[l], s, nullptr, &cams[v0 + w], &targets[v0 + w], nullptr,
+                     reinterpret_cast<gs_stream>(c->lane_stream[l]), &pre);
+    if (r != GS_SUCCESS) return r;
+  }
+  return join_lanes(c, used, st);
+}
+
+gs_status gs_context_set_batch_shared_cull(gs_context* c, int enable) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  c->multi_view_cull = enable != 0;
+  return GS_SUCCESS;
+}
+
 gs_status gs_render_batched(gs_context* c, const gs_splats* s, uint32_t n_views, const gs_camera* cams,
                             const gs_target* targets, gs_stream stream) {
   if (!c || !s || (n_views && (!cams || !targets))) return GS_ERROR_INVALID_ARGUMENT;
@@ -949,6 +1084,17 @@ gs_status gs_render_batched(gs_context* c, const gs_splats* s, uint32_t n_views,
       const gs_status r = gs_render(c, s, &cams[v], &targets[v], nullptr, stream);
       if (r != GS_SUCCESS) return r;
     }
+    return GS_SUCCESS;
+  }
+  if (s->count && (!s->position || !s->cov3d || !s->opacity || !s->sh)) return GS_ERROR_INVALID_ARGUMENT;
+  if ((reinterpret_cast<uintptr_t>(s->sh) & 15u) != 0) return GS_ERROR_INVALID_ARGUMENT;
+  if (s->count > c->max_splats || s->count > 0x3fffffffu) return GS_ERROR_CAPACITY;
+  if (s->count > 0 && c->multi_view_cull && batch_buffers(c, std::min(n_views, kMaxBatchViews), st)) {
+    for (u32 v0 = 0; v0 < n_views; v0 += c->batch_views) {  // groups share the per-view buffers
+      const gs_status r = batched_group(c, s, v0, std::min(c->batch_views, n_views - v0), cams, targets, st);
+      if (r != GS_SUCCESS) return r;
+    }
+    c->last_batched = true;
     return GS_SUCCESS;
   }
   const u32 used = std::min(c->nlanes, std::max(n_views, 1u));

@@ -243,6 +243,105 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
   }
 }
 
+// Many views of the same splats in one pass (the batched form): each partition's positions are loaded
+// once, every view's visibility and ballots are taken from them, thread v of the first warp resolves
+// view v's look-back, and each visible (splat, view) is keyed and projected into that view's buffers.
+// The splat's covariance, opacity and SH are read once per partition from DRAM and then from cache for
+// the other views.  Outputs are bit-identical to k_cull_project<false> run per view.
+__global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs a) {
+  __shared__ u32 s_cnt[kMaxCullViews][kCullItems][kCullThreads / 32];
+  __shared__ u32 s_base[kMaxCullViews];
+  __shared__ u32 s_part;
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const u32 n = a.n, nv = a.count;
+  const u32 nparts = (n + kCullTile - 1) / kCullTile;
+  const u32 lt = lanemask_lt();
+  CullArgs ca{};  // the shared inputs; the record pointer is set per view
+  ca.position = a.position;
+  ca.cov3d = a.cov3d;
+  ca.opacity = a.opacity;
+  ca.sh = a.sh;
+  for (;;) {
+    if (tid == 0) s_part = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    const u32 p = s_part;
+    if (p >= nparts) break;
+    float px[kCullItems], py[kCullItems], pz[kCullItems];
+    u32 visbits[kCullItems];
+#pragma unroll
+    for (u32 k = 0; k < kCullItems; ++k) {
+      const u32 id = p * kCullTile + k * kCullThreads + tid;
+      px[k] = py[k] = pz[k] = 0.0f;
+      visbits[k] = 0;
+      if (id < n) {
+        px[k] = __ldg(a.position + 3 * (size_t)id + 0);
+        py[k] = __ldg(a.position + 3 * (size_t)id + 1);
+        pz[k] = __ldg(a.position + 3 * (size_t)id + 2);
+      }
+    }
+#pragma unroll 1
+    for (u32 v = 0; v < nv; ++v) {
+#pragma unroll
+      for (u32 k = 0; k < kCullItems; ++k) {
+        bool vis = false;
+        if (p * kCullTile + k * kCullThreads + tid < n) {
+          const float q[4] = {px[k], py[k], pz[k], 1.0f};
+          float c[4];
+          mat4_vec4(a.fc[v].pvm, q, c);
+          const float x = c[0] / c[3], y = c[1] / c[3], z = c[2] / c[3];
+          vis = fabsf(x) <= 1.0f && fabsf(y) <= 1.0f && z >= 0.0f && z <= 1.0f;
+        }
+        visbits[k] |= (vis ? 1u : 0u) << v;
+        const u32 ball = __ballot_sync(0xffffffffu, vis);
+        if (lane == 0) s_cnt[v][k][warp] = __popc(ball);
+      }
+    }
+    __syncthreads();
+    if (tid < nv) {  // view tid: offsets of its warps, look-back over the partitions
+      u32 acc = 0;
+      for (u32 k = 0; k < kCullItems; ++k)
+        for (u32 w = 0; w < kCullThreads / 32; ++w) {
+          const u32 c = s_cnt[tid][k][w];
+          s_cnt[tid][k][w] = acc;
+          acc += c;
+        }
+      const u32 excl = lookback(a.view[tid].status, 1, p, a.epoch, acc, a.err);
+      s_base[tid] = excl;
+      if (p == nparts - 1) *a.view[tid].visible_count = excl + acc;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (u32 k = 0; k < kCullItems; ++k) {
+      const u32 id = p * kCullTile + k * kCullThreads + tid;
+#pragma unroll 1
+      for (u32 v = 0; v < nv; ++v) {
+        const bool vis = (visbits[k] >> v) & 1u;
+        const u32 ball = __ballot_sync(0xffffffffu, vis);
+        if (vis) {
+          const float q[4] = {px[k], py[k], pz[k], 1.0f};
+          float c[4];
+          mat4_vec4(a.fc[v].pvm, q, c);
+          const u32 slot = s_base[v] + s_cnt[v][k][warp] + __popc(ball & lt);
+          a.view[v].key[slot] = __float_as_uint(1.0f - c[2] / c[3]);
+          a.view[v].index[slot] = id;
+          ca.record = a.view[v].record;
+          project_splat<false>(a.fc[v], ca, id, px[k], py[k], pz[k]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_cull_views(const CullViewsArgs& a, cudaStream_t stream) {
+  if (a.n == 0 || a.count == 0) return cudaSuccess;
+  if (a.count > kMaxCullViews) return cudaErrorInvalidValue;
+  const u32 parts = (a.n + kCullTile - 1) / kCullTile;
+  const int sms = a.num_sms > 0 ? a.num_sms : 1;
+  k_cull_views<<<min(parts, (u32)sms * 8u), kCullThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 const void* cull_project_kernel() { return reinterpret_cast<const void*>(&k_cull_project<false>); }
 
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream) {

@@ -58,6 +58,31 @@ struct CullArgs {
   int num_sms;
 };
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
+
+// The cull + projection of up to kMaxCullViews views of the same splats in one launch (binary16 SH).
+constexpr u32 kMaxCullViews = 32;
+struct CullView {
+  u32* key;            // compacted keys / ids of the view, ascending id
+  u32* index;
+  float4* record;      // N x 4 float4, indexed by id
+  u32* visible_count;
+  u64* status;         // >= ceil(N / kCullTile) words, cleared (epoch-tagged like CullArgs.status)
+};
+struct CullViewsArgs {
+  const float* position;
+  const float* cov3d;
+  const float* opacity;
+  const uint16_t* sh;
+  u32 n;
+  u32 count;  // views
+  u32* ticket;
+  u32 epoch;
+  u32* err;
+  int num_sms;
+  FrameConst fc[kMaxCullViews];
+  CullView view[kMaxCullViews];
+};
+cudaError_t launch_cull_views(const CullViewsArgs& a, cudaStream_t stream);
 const void* cull_project_kernel();  // the plain path's cull kernel (the only one reading the camera)
 
 // Gathers instance records into sorted order and writes the indirect draw arguments.
