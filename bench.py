@@ -249,12 +249,16 @@ def batched_differentiation_form(dev, quick: bool = False):
     import torch
     from vkgs_gb300 import Camera, Renderer, synthetic as syn, train, train_params as tp
 
+    import gc
+
     rows, _, specs = syn.workload("batched_grad")
     raw = tp.from_rows(rows)
     n = rows.shape[0]
     del rows
     cams = [Camera.from_spec(sp) for sp in specs]
+    gc.collect()  # renderers of earlier forms
     torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     free0, total = torch.cuda.mem_get_info()
     params = {k: torch.tensor(v, device=dev, requires_grad=True) for k, v in raw.items()}
     mw, mh = max(c.width for c in cams), max(c.height for c in cams)
@@ -289,9 +293,10 @@ def batched_differentiation_form(dev, quick: bool = False):
     step_ms = timed(step)
     r.check()
     free1, _ = torch.cuda.mem_get_info()
-    # device memory outside torch's caching allocator (the renderer's arenas, CUDA context) + torch's peak
+    # device memory outside torch's caching allocator (the renderer's arenas, CUDA context) + torch's peak,
+    # less what was in use before the form started
     outside = (total - free1) - torch.cuda.memory_reserved()
-    peak_gb = (outside + torch.cuda.max_memory_reserved()) / 1e9
+    peak_gb = (outside + torch.cuda.max_memory_reserved() - (total - free0)) / 1e9
     single = Renderer(n, mw, mh)
 
     def loop():
@@ -308,7 +313,7 @@ def batched_differentiation_form(dev, quick: bool = False):
                         "accumulated into one per-splat buffer",
             "fwd_bwd_it_per_s": 1e3 / step_ms, "ms_fwd_bwd": step_ms, "views_per_s": len(cams) * 1e3 / step_ms,
             "per_view_loop_ms": loop_ms, "speedup_vs_per_view_loop": loop_ms / step_ms,
-            "peak_hbm_gb": peak_gb, "hbm_before_gb": (total - free0) / 1e9,
+            "peak_hbm_gb": peak_gb, "device_in_use_before_gb": (total - free0) / 1e9,
             "form": "torch.autograd.Function over gs_train_forward_batched / gs_train_backward_batched "
                     "(one render lane per view; per-tile recomputation in the blend backward, per-pixel state "
                     "= final transmittance + blended count)"}
