@@ -62,13 +62,15 @@ __device__ __forceinline__ u64 lb_pack(u32 epoch, u32 flag, u32 value) {
 // One thread's look-back for partition p over status words status[j * stride] (j < p).  Publishes
 // `aggregate`, walks back until an inclusive prefix is found, publishes its own inclusive prefix and
 // returns the exclusive prefix.  Every wait is bounded by kMaxSpins.
-__device__ __forceinline__ u32 lookback(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
+__device__ __forceinline__ void lb_publish(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate) {
+  st_relaxed_u64(status + (size_t)p * stride, lb_pack(epoch, p == 0 ? LB_INCLUSIVE : LB_AGGREGATE, aggregate));
+}
+
+// The second half of lookback(), after lb_publish(aggregate): walks back, publishes the inclusive
+// prefix and returns the exclusive one.
+__device__ __forceinline__ u32 lb_resolve(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
+  if (p == 0) return 0;
   u64* mine = status + (size_t)p * stride;
-  if (p == 0) {
-    st_relaxed_u64(mine, lb_pack(epoch, LB_INCLUSIVE, aggregate));
-    return 0;
-  }
-  st_relaxed_u64(mine, lb_pack(epoch, LB_AGGREGATE, aggregate));
   u32 exclusive = 0;
   int j = (int)p - 1;
   u32 spins = 0;
@@ -89,6 +91,11 @@ __device__ __forceinline__ u32 lookback(u64* status, u32 stride, u32 p, u32 epoc
   }
   st_relaxed_u64(mine, lb_pack(epoch, LB_INCLUSIVE, exclusive + aggregate));
   return exclusive;
+}
+
+__device__ __forceinline__ u32 lookback(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
+  lb_publish(status, stride, p, epoch, aggregate);
+  return lb_resolve(status, stride, p, epoch, aggregate, err);
 }
 
 // Exclusive scan of one value per thread across a block of NT threads (NT multiple of 32, <= 1024).

@@ -180,25 +180,23 @@ template <bool SH32>
 __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameConst fc, const CullArgs a) {
   __shared__ u32 s_cnt[kCullItems][kCullThreads / 32];
   __shared__ u32 s_off[kCullItems][kCullThreads / 32];
-  __shared__ u32 s_base;
+  __shared__ u32 s_key[kCullItems][kCullThreads];  // keys wait here while the partition projects
+  __shared__ u32 s_base, s_acc;
   __shared__ u32 s_part;
   const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const u32 n = fc.n;
   const u32 nparts = (n + kCullTile - 1) / kCullTile;
-  const u32 lt = lanemask_lt();
   for (;;) {
     if (tid == 0) s_part = atomicAdd(a.ticket, 1u);
     __syncthreads();
     const u32 p = s_part;
     if (p >= nparts) break;
     float px[kCullItems], py[kCullItems], pz[kCullItems];
-    u32 key[kCullItems], ball[kCullItems];
     bool vis[kCullItems];
 #pragma unroll
     for (u32 k = 0; k < kCullItems; ++k) {
       const u32 id = p * kCullTile + k * kCullThreads + tid;
       vis[k] = false;
-      key[k] = 0;
       px[k] = py[k] = pz[k] = 0.0f;
       if (id < n) {
         px[k] = __ldg(a.position + 3 * (size_t)id + 0);
@@ -209,12 +207,15 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
         mat4_vec4(fc.pvm, v, c);
         const float x = c[0] / c[3], y = c[1] / c[3], z = c[2] / c[3];
         vis[k] = fabsf(x) <= 1.0f && fabsf(y) <= 1.0f && z >= 0.0f && z <= 1.0f;
-        key[k] = __float_as_uint(1.0f - z);
+        s_key[k][tid] = __float_as_uint(1.0f - z);
       }
-      ball[k] = __ballot_sync(0xffffffffu, vis[k]);
-      if (lane == 0) s_cnt[k][warp] = __popc(ball[k]);
+      const u32 ball = __ballot_sync(0xffffffffu, vis[k]);
+      if (lane == 0) s_cnt[k][warp] = __popc(ball);
     }
     __syncthreads();
+    // The partition's aggregate is published at once; its look-back is resolved after the projection
+    // (which writes by id and needs no offset), so the wait overlaps with work.  What the key writes
+    // need afterwards is re-read from shared memory, so little stays live across the projection calls.
     if (tid == 0) {
       u32 acc = 0;
       for (u32 k = 0; k < kCullItems; ++k)
@@ -222,23 +223,33 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
           s_off[k][w] = acc;
           acc += s_cnt[k][w];
         }
-      const u32 excl = lookback(a.status, 1, p, a.epoch, acc, a.err);
+      s_acc = acc;
+      lb_publish(a.status, 1, p, a.epoch, acc);
+    }
+    {
+      const u32 id0 = p * kCullTile + tid;
+#pragma unroll 1
+      for (u32 k = 0; k < kCullItems; ++k)
+        if (vis[k]) project_splat<SH32>(fc, a, id0 + k * kCullThreads, px[k], py[k], pz[k]);
+    }
+    const u32 t = threadIdx.x, pp = *reinterpret_cast<volatile u32*>(&s_part);
+    if (t == 0) {
+      const u32 acc = s_acc;
+      const u32 excl = lb_resolve(a.status, 1, pp, a.epoch, acc, a.err);
       s_base = excl;
-      if (p == nparts - 1) *a.visible_count = excl + acc;
+      if (pp == nparts - 1) *a.visible_count = excl + acc;
     }
     __syncthreads();
+    const u32 ltm = lanemask_lt();
 #pragma unroll
     for (u32 k = 0; k < kCullItems; ++k) {
+      const u32 ball = __ballot_sync(0xffffffffu, vis[k]);
       if (vis[k]) {
-        const u32 id = p * kCullTile + k * kCullThreads + tid;
-        const u32 slot = s_base + s_off[k][warp] + __popc(ball[k] & lt);
-        a.key[slot] = key[k];
-        a.index[slot] = id;
+        const u32 slot = s_base + s_off[k][t >> 5] + __popc(ball & ltm);
+        a.key[slot] = s_key[k][t];
+        a.index[slot] = pp * kCullTile + k * kCullThreads + t;
       }
     }
-#pragma unroll 1
-    for (u32 k = 0; k < kCullItems; ++k)
-      if (vis[k]) project_splat<SH32>(fc, a, p * kCullTile + k * kCullThreads + tid, px[k], py[k], pz[k]);
     __syncthreads();
   }
 }

@@ -47,7 +47,7 @@ __global__ __launch_bounds__(256) void k_radix_histogram(const u32* __restrict__
 }
 
 template <bool HAS_VALUES>
-__global__ __launch_bounds__(RS_THREADS, 3) void k_radix_onesweep(
+__global__ __launch_bounds__(RS_THREADS, 4) void k_radix_onesweep(
     const u32* __restrict__ keys_in, u32* __restrict__ keys_out, const u32* __restrict__ vals_in,
     u32* __restrict__ vals_out, const u32* __restrict__ count_ptr, u32 max_count, const u32* __restrict__ hist,
     u64* __restrict__ status, u32* __restrict__ ticket, u32 epoch, u32 shift, u32* __restrict__ err) {
