@@ -255,13 +255,14 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
 }
 
 // Many views of the same splats in one pass (the batched form): each partition's positions are loaded
-// once, every view's visibility and ballots are taken from them, thread v of the first warp resolves
-// view v's look-back, and each visible (splat, view) is keyed and projected into that view's buffers.
+// once, every view's visibility and ballots are taken from them, thread v of the first warp publishes
+// and later resolves view v's look-back, each visible (splat, view) is projected into that view's
+// records, and then keyed into its compacted lists.
 // The splat's covariance, opacity and SH are read once per partition from DRAM and then from cache for
 // the other views.  Outputs are bit-identical to k_cull_project<false> run per view.
 __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs a) {
   __shared__ u32 s_cnt[kMaxCullViews][kCullItems][kCullThreads / 32];
-  __shared__ u32 s_base[kMaxCullViews];
+  __shared__ u32 s_base[kMaxCullViews], s_acc[kMaxCullViews];
   __shared__ u32 s_part;
   const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const u32 n = a.n, nv = a.count;
@@ -308,7 +309,7 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs
       }
     }
     __syncthreads();
-    if (tid < nv) {  // view tid: offsets of its warps, look-back over the partitions
+    if (tid < nv) {  // view tid: offsets of its warps; its aggregate is published now, resolved later
       u32 acc = 0;
       for (u32 k = 0; k < kCullItems; ++k)
         for (u32 w = 0; w < kCullThreads / 32; ++w) {
@@ -316,7 +317,24 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs
           s_cnt[tid][k][w] = acc;
           acc += c;
         }
-      const u32 excl = lookback(a.view[tid].status, 1, p, a.epoch, acc, a.err);
+      s_acc[tid] = acc;
+      lb_publish(a.view[tid].status, 1, p, a.epoch, acc);
+    }
+    // project every visible (splat, view) -- records are written by id and need no offset
+#pragma unroll 1
+    for (u32 k = 0; k < kCullItems; ++k) {
+      const u32 id = p * kCullTile + k * kCullThreads + tid;
+#pragma unroll 1
+      for (u32 v = 0; v < nv; ++v) {  // the same view across the warp: no divergence between views
+        if ((visbits[k] >> v) & 1u) {
+          ca.record = a.view[v].record;
+          project_splat<false>(a.fc[v], ca, id, px[k], py[k], pz[k]);
+        }
+      }
+    }
+    if (tid < nv) {
+      const u32 acc = s_acc[tid];
+      const u32 excl = lb_resolve(a.view[tid].status, 1, p, a.epoch, acc, a.err);
       s_base[tid] = excl;
       if (p == nparts - 1) *a.view[tid].visible_count = excl + acc;
     }
@@ -335,8 +353,6 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs
           const u32 slot = s_base[v] + s_cnt[v][k][warp] + __popc(ball & lt);
           a.view[v].key[slot] = __float_as_uint(1.0f - c[2] / c[3]);
           a.view[v].index[slot] = id;
-          ca.record = a.view[v].record;
-          project_splat<false>(a.fc[v], ca, id, px[k], py[k], pz[k]);
         }
       }
     }
