@@ -499,19 +499,42 @@ def run_ours(args):
     ms_max = float(t.item())
     value = world * K / (ms_max / 1000.0)
 
-    # End to end through the public API: per step the camera crosses into the graph (h2d, the cull
-    # node's parameters) and the finished RGBA image is copied into pinned host memory (d2h).
-    host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
-    barrier()
+    # End to end through the public API, as a viewer presents its frames: per step the camera crosses
+    # into the graph (h2d, the cull node's parameters) and the finished RGBA image is copied into pinned
+    # host memory (d2h).  Two targets alternate (two viewers of the same renderer) so that frame k's copy,
+    # on a copy stream, overlaps frame k+1's rendering; a target is drawn into again only after its
+    # previous copy has finished.
+    colors = [color, torch.empty_like(color)]
+    viewers = [viewer, Viewer(r, splats, cams[0], colors[1])]
+    hosts = [torch.empty((H, W, 4), dtype=torch.float32).pin_memory() for _ in range(2)]
+    main, copier = torch.cuda.current_stream(), torch.cuda.Stream()
+    rendered = [torch.cuda.Event() for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
+
+    def present(k):
+        b = k & 1
+        if k >= 2:
+            main.wait_event(copied[b])
+        viewers[b].frame(cams[k % len(cams)], stream=main)
+        rendered[b].record(main)
+        copier.wait_event(rendered[b])
+        with torch.cuda.stream(copier):
+            hosts[b].copy_(colors[b], non_blocking=True)
+        copied[b].record(copier)
+
+    for k in range(max(args.warmup, 3)):
+        present(k)
     torch.cuda.synchronize()
-    e0.record()
+    barrier()
+    e0.record(main)
     for k in range(K):
-        viewer.frame(cams[k % len(cams)])
-        host.copy_(color, non_blocking=True)
-    e1.record()
+        present(k)
+    main.wait_stream(copier)
+    e1.record(main)
     torch.cuda.synchronize()
     barrier()
-    viewer.close()
+    for v in viewers:
+        v.close()
     r.check()
     te = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
     if dist is not None:
@@ -571,7 +594,9 @@ def run_ours(args):
                                "(8 on an r=8 circle + 1 at r=20), SH degree 3 in binary16",
                    "parallelism": f"replicas x{world}", "l2": "inputs (816 MB) exceed L2; no flush",
                    "depth_slabs": "nearest 128/1024 of the visible splats, then the rest"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 292, "d2h_bytes_per_step": H * W * 16},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 292, "d2h_bytes_per_step": H * W * 16,
+                "form": "gs_viewer_frame per step + the RGBA image copied to pinned host memory; two targets "
+                        "alternate so frame k's copy overlaps frame k+1's rendering"},
         "gpu_launches": None,
         "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
                      "unit": "T lane-ops/s", "frac": achieved / fp32_peak, "traffic": profile_traffic(),
