@@ -303,6 +303,12 @@ gs_status gs_context_enable_timing(gs_context* context, int enable);
  * the number of rows written. */
 gs_status gs_context_stage_times(gs_context* context, uint32_t max_frames, float* ms, uint32_t* frames);
 
+/* Test support (no reference counterpart): runs one bounded device-side wait on a status word that
+ * nothing publishes, so the wait gives up (after about a second of polling) exactly as a look-back
+ * whose predecessor never arrives would; synchronises `stream` and returns GS_ERROR_DEVICE_TIMEOUT
+ * when the wait recorded its timeout.  Nothing faults, and the device stays usable afterwards. */
+gs_status gs_selftest_bounded_wait(gs_stream stream);
+
 /* Synchronises the stream, then returns (and clears) the device error word of the last frames:
  * GS_ERROR_CAPACITY when the tile pairs overflowed (stats->tile_pairs says how many are needed),
  * GS_ERROR_DEVICE_TIMEOUT when a bounded wait gave up.  stats may be NULL. */

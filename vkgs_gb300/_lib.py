@@ -96,6 +96,7 @@ SIGNATURES = [
     ("gs_render", c_int,
      [c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), POINTER(GsFrameOutputs), c_void_p]),
     ("gs_context_check", c_int, [c_void_p, c_void_p, POINTER(GsFrameStats)]),
+    ("gs_selftest_bounded_wait", c_int, [c_void_p]),
     ("gs_train_forward", c_int, [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, c_void_p]),
     ("gs_train_backward", c_int,
      [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, POINTER(GsTrainGrads), c_void_p]),

@@ -1125,6 +1125,22 @@ gs_status gs_render_batched(gs_context* c, const gs_splats* s, uint32_t n_views,
   return GS_SUCCESS;
 }
 
+gs_status gs_selftest_bounded_wait(gs_stream stream) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  void* buf = nullptr;  // 2 status words + the error word
+  if (cudaMalloc(&buf, 3 * sizeof(u64)) != cudaSuccess) return GS_ERROR_OUT_OF_MEMORY;
+  u32 e = 0;
+  const bool ok = cudaMemsetAsync(buf, 0, 3 * sizeof(u64), st) == cudaSuccess &&
+                  launch_wait_selftest(static_cast<u64*>(buf), reinterpret_cast<u32*>(static_cast<u64*>(buf) + 2),
+                                       st) == cudaSuccess &&
+                  cudaMemcpyAsync(&e, static_cast<u64*>(buf) + 2, sizeof(u32), cudaMemcpyDeviceToHost, st) ==
+                      cudaSuccess &&
+                  cudaStreamSynchronize(st) == cudaSuccess;
+  cudaFree(buf);
+  if (!ok) return GS_ERROR_CUDA;
+  return (e & ERR_TIMEOUT) ? GS_ERROR_DEVICE_TIMEOUT : GS_SUCCESS;
+}
+
 gs_status gs_context_check(gs_context* c, gs_stream stream, gs_frame_stats* stats) {
   if (!c) return GS_ERROR_INVALID_ARGUMENT;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);

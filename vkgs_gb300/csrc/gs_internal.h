@@ -34,6 +34,8 @@ size_t radix_status_words(u32 max_count);
 // Sorts keys[0..*count) (and values) on bits [begin_bit, end_bit).  After an odd number of passes the
 // result lies in keys_alt / values_alt.
 cudaError_t radix_sort(const RadixSortArgs& a, cudaStream_t stream);
+// One look-back wait that runs out (status: 2 zeroed words, err: zeroed word); for tests.
+cudaError_t launch_wait_selftest(u64* status, u32* err, cudaStream_t stream);
 
 // ---- cull + key + compaction + projection (gs_cull.cu) ----
 constexpr u32 kCullThreads = 256;

@@ -138,6 +138,18 @@ __global__ __launch_bounds__(RS_THREADS, 4) void k_radix_onesweep(
   }
 }
 
+// The failure path of a bounded wait, for tests: partition 1 looks back at partition 0, which never
+// publishes (its status word stays zero, an epoch no pass uses), so the wait gives up after kMaxSpins
+// polls, records ERR_TIMEOUT and the kernel returns.
+__global__ void k_wait_selftest(u64* status, u32* err) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) lookback(status, 1, 1, 0x5e1f7e57u, 1u, err);
+}
+
+cudaError_t launch_wait_selftest(u64* status, u32* err, cudaStream_t stream) {
+  k_wait_selftest<<<1, 32, 0, stream>>>(status, err);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------
 // Host side.
 
