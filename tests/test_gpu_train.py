@@ -152,3 +152,38 @@ def test_batched_train_needs_a_lane_per_view(cuda):
     imgs = train.forward_batched(r, tensors, [cam] * 3)  # the Python side adds lanes
     assert r.batch_lanes == 3 and len(imgs) == 3
     r.check()
+
+
+def test_sharded_train_step_single_rank_matches_batched(cuda):
+    """The data-parallel step (vkgs_gb300.shard.train_step_sharded) at world size 1 over NCCL: its
+    all-reduced gradients equal the batched Function's."""
+    import socket
+
+    import torch
+    import torch.distributed as dist
+    from vkgs_gb300 import Camera, Renderer, shard, train
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    dist.init_process_group("nccl", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        n = 5_000
+        rows = syn.splat_rows(n, 31)
+        cams = [Camera.from_spec(sp) for sp in syn.random_cameras(3, seed=507, resolutions=[(160, 120), (128, 96)])]
+        gen = torch.Generator(device="cuda").manual_seed(8)
+        targets = [torch.rand((c.height, c.width, 4), device="cuda", generator=gen) for c in cams]
+        r = Renderer(n, 160, 120)
+        r.set_batch_lanes(len(cams))
+        p1 = _gpu_params(rows)
+        loss = shard.train_step_sharded(p1, cams, lambda v, img: (img - targets[v]).abs().mean(), r, 0, 1)
+        p2 = _gpu_params(rows)
+        imgs = train.render_batched(p2, cams, Renderer(n, 160, 120))
+        ref = sum((img - t).abs().mean() for img, t in zip(imgs, targets))
+        ref.backward()
+        assert abs(float(loss) - float(ref.detach())) <= 1e-5 * abs(float(ref.detach()))
+        for k in train.NAMES:
+            rel = float((p1[k].grad - p2[k].grad).norm() / p2[k].grad.norm())
+            assert rel <= 1e-5, (k, rel)
+    finally:
+        dist.destroy_process_group()
