@@ -158,8 +158,9 @@ typedef struct gs_context_options {
 
 typedef struct gs_frame_stats {
   uint32_t visible_count;     /* V of the last frame */
-  uint32_t tile_pairs;        /* largest (splat, tile) pair count of one depth slab of the last frame:
-                                 the max_tile_pairs capacity that frame needed */
+  uint32_t tile_pairs;        /* the max_tile_pairs capacity the last frame needed: its largest depth
+                                 slab's (splat, tile) pairs (the differentiable path with stacked slabs:
+                                 all slabs' pairs together) */
   uint64_t fragments;         /* covered (pixel, splat) pairs passing the depth test: the fragment-shader
                                  invocations of the reference's draw; only with
                                  gs_context_set_count_fragments(1) */
@@ -249,11 +250,18 @@ typedef struct gs_train_grads {
   float* sh;
 } gs_train_grads;
 
-/* The frame of gs_render (one depth slab, no caller depth) from raw parameters into an RGBA float
+/* The frame of gs_render (no caller depth) from raw parameters into an RGBA float
  * target, keeping in the context what gs_train_backward needs: the activated splats, the tile lists,
  * and per pixel its final transmittance and how many list entries it blended (each pixel stops
  * exactly when its transmittance falls below the context's transmittance floor, so the image and the
- * gradients leave out contributions smaller than the floor).  Valid until the context renders again. */
+ * gradients leave out contributions smaller than the floor).  From a splat count on (default 2^20,
+ * gs_context_set_train_slab_min) it uses the context's depth-slab schedule and keeps every slab's tile
+ * lists (the pair capacity must then hold all slabs' pairs together; gs_frame_stats.tile_pairs reports
+ * that need); below it, one slab.  Valid until the context renders again. */
+/* Smallest splat count at which the differentiable forward uses depth slabs (default 2^20: below it
+ * the per-slab fixed cost outweighs the pairs the slabs save). */
+gs_status gs_context_set_train_slab_min(gs_context* context, uint32_t splats);
+
 gs_status gs_train_forward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
                            float* color_rgba32f, gs_stream stream);
 

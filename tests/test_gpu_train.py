@@ -22,8 +22,13 @@ def _gpu_params(rows, f16_sh=False):
     return {k: torch.tensor(v, device="cuda", requires_grad=True) for k, v in p.items()}
 
 
-@pytest.mark.parametrize("n,w,h,eye,seed", [(1000, 128, 128, (0.0, 0.0, 6.0), 3), (400, 96, 80, (1.5, 0.5, 4.0), 5)])
-def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed):
+@pytest.mark.parametrize("n,w,h,eye,seed,slabs", [
+    (1000, 128, 128, (0.0, 0.0, 6.0), 3, None),
+    (400, 96, 80, (1.5, 0.5, 4.0), 5, None),
+    (1000, 128, 128, (0.0, 0.0, 6.0), 3, (128, 1024)),       # stacked slabs: every slab's lists kept
+    (3000, 112, 96, (1.0, -0.5, 5.0), 6, (64, 320, 1024)),
+])
+def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed, slabs):
     import torch
     from oracle import torch_ref
     from vkgs_gb300 import train
@@ -40,6 +45,9 @@ def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed):
     from vkgs_gb300 import Renderer
 
     r = Renderer(n, w, h)
+    if slabs is not None:
+        r.set_slabs(slabs)
+        r.set_train_slab_min(0)
     img = train.render(params, scenes.product_camera(c), r)
     (img * torch.tensor(weights, dtype=torch.float32, device="cuda")).sum().backward()
 
@@ -119,6 +127,7 @@ def test_batched_gradients_equal_sum_of_views(cuda, oracle):
 
     r = Renderer(n, 200, 160)
     r.set_batch_lanes(len(cams))
+    r.set_train_slab_min(0)  # stacked depth slabs on the lanes; the one-view reference uses one slab
     params = _gpu_params(rows)
     imgs = train.render_batched(params, cams, r)
     sum((img * wt).sum() for img, wt in zip(imgs, weights)).backward()

@@ -97,6 +97,7 @@ SIGNATURES = [
      [c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), POINTER(GsFrameOutputs), c_void_p]),
     ("gs_context_check", c_int, [c_void_p, c_void_p, POINTER(GsFrameStats)]),
     ("gs_selftest_bounded_wait", c_int, [c_void_p]),
+    ("gs_context_set_train_slab_min", c_int, [c_void_p, c_uint32]),
     ("gs_train_forward", c_int, [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, c_void_p]),
     ("gs_train_backward", c_int,
      [c_void_p, POINTER(GsTrainParams), POINTER(GsCamera), c_void_p, POINTER(GsTrainGrads), c_void_p]),

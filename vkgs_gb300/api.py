@@ -196,6 +196,10 @@ class Renderer:
         _check(self._lib.gs_context_set_transmittance_floor(self._h, float(t_floor)),
                "gs_context_set_transmittance_floor")
 
+    def set_train_slab_min(self, splats: int = 1 << 20) -> None:
+        """Splat count from which the differentiable forward uses the depth-slab schedule."""
+        _check(self._lib.gs_context_set_train_slab_min(self._h, int(splats)), "set_train_slab_min")
+
     def count_fragments(self, enable: bool = True) -> None:
         _check(self._lib.gs_context_set_count_fragments(self._h, int(bool(enable))), "count_fragments")
 

@@ -96,7 +96,13 @@ struct gs_context {
   float* train_pos = nullptr;      // activated splats of the last gs_train_forward
   float* train_cov = nullptr;
   float* train_opacity = nullptr;
-  u32* train_nproc = nullptr;      // per pixel: list entries blended
+  u32* train_nproc = nullptr;      // per slab and pixel: list entries blended
+  u32 train_slabs = 1;             // depth slabs of the last differentiable forward
+  // The differentiable forward uses the slab schedule from this many splats on; below it the per-slab
+  // fixed cost (seven more launches, the blended-count clears) outweighs the pairs it saves (measured:
+  // 200k splats at 800x800, one slab 0.86 ms per fwd+bwd step vs 0.94 ms with two; 3M splats x 16
+  // views, two slabs 29.9 ms vs 32.1 ms).
+  u32 train_slab_min = 1u << 20;
   float* grad_rec = nullptr;       // per splat blend gradients (kGradRec floats)
   float4* state_c = nullptr;  // running pixel sums between depth slabs
   float* state_t = nullptr;
@@ -151,13 +157,13 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->bin_count = cv.take<u32>(n);
     t->bin_diff = cv.take<u32>(bin_diff_words(tiles_x, tiles_y));
     t->giant_list = cv.take<u32>(n);
-    t->tile_range = cv.take<u32>((size_t)(max_tiles + 1) * 2);
+    t->tile_range = cv.take<u32>((size_t)GS_MAX_SLABS * (max_tiles + 1) * 2);  // one per slab (stacked)
     t->tile_done = cv.take<u32>((max_tiles + 31) / 32);
     t->tile_order = cv.take<u32>(max_tiles);
     t->train_pos = cv.take<float>((size_t)n * 3);
     t->train_cov = cv.take<float>((size_t)n * 6);
     t->train_opacity = cv.take<float>(n);
-    t->train_nproc = cv.take<u32>((size_t)max_width * max_height);
+    t->train_nproc = cv.take<u32>((size_t)GS_MAX_SLABS * max_width * max_height);  // per slab
     t->grad_rec = cv.take<float>((size_t)n * kGradRec);
     t->state_c = cv.take<float4>((size_t)max_width * max_height);
     t->state_t = cv.take<float>((size_t)max_width * max_height);
@@ -505,6 +511,13 @@ gs_status gs_context_set_slabs(gs_context* c, uint32_t count, const uint32_t* en
   return GS_SUCCESS;
 }
 
+gs_status gs_context_set_train_slab_min(gs_context* c, uint32_t splats) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  c->train_slab_min = splats;
+  for (u32 l = 0; l < c->nlanes; ++l) c->lane[l]->train_slab_min = splats;
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_set_transmittance_floor(gs_context* c, float t_floor) {
   if (!c || !(t_floor > 0.0f) || !(t_floor <= 1.0f / 255.0f)) return GS_ERROR_INVALID_ARGUMENT;
   c->t_floor = t_floor;
@@ -519,6 +532,9 @@ gs_status gs_context_set_count_fragments(gs_context* c, int enable) {
   return GS_SUCCESS;
 }
 
+// Words of one slab's tile-range array at the context's capacity (tiles + 1 entries of 2 words).
+static size_t range_words(const gs_context* c) { return (size_t)(c->max_tiles + 1) * 2; }
+
 // A view culled and projected beforehand (k_cull_views): its compacted keys/ids, records, visible count.
 struct PreCulled {
   u32* key;
@@ -527,8 +543,8 @@ struct PreCulled {
   u32* visible;
 };
 
-// One frame.  sh32 (the differentiable path): FP32 SH instead of s->sh, one depth slab, and the
-// training raster that stores per-pixel blend counts and final transmittance.  pre: the cull already
+// One frame.  sh32 (the differentiable path): FP32 SH instead of s->sh, every slab's tile lists kept
+// (stacked), and the training raster that stores per-pixel blend counts and final transmittance.  pre: the cull already
 // ran for this view (the batched form); the frame starts at the depth sort on pre's buffers.
 static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh32, const gs_camera* cam,
                               const gs_target* t, const gs_frame_outputs* outs, gs_stream stream,
@@ -608,8 +624,17 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     GS_TRY(launch_instances(index, visible, c->inst_by_id, n, o.instances, o.draw_indirect, st));
   GS_MARK(2);
 
-  // Depth slabs, nearest first (one slab when nothing is visible).
-  const u32 slabs = (n > 0 && !train) ? c->slab_count : 1;
+  // Depth slabs, nearest first (one slab when nothing is visible).  The differentiable forward keeps
+  // every slab's tile lists (stacked in the pair arrays, a tile-range array per slab) and blended
+  // counts for its backward.
+  const u32 slabs = (n > 0 && (!train || n >= c->train_slab_min)) ? c->slab_count : 1;
+  const size_t range_stride = range_words(c);
+  const size_t pix_stride = (size_t)c->max_width * c->max_height;
+  if (train) {
+    c->train_slabs = slabs;
+    for (u32 k = 1; k < slabs; ++k)  // tiles finished earlier are skipped by later slabs: count 0
+      GS_TRY(cudaMemsetAsync(c->train_nproc + k * pix_stride, 0, (size_t)W * H * sizeof(u32), st));
+  }
   if (ev) c->frame_slabs[(c->timed_frames - 1) % gs_context::kTimingRing] = slabs;
   for (u32 k = 0; k < slabs; ++k) {
     const int e = 3 + 4 * (int)k;
@@ -627,7 +652,8 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     ba.tiles_y = tiles_y;
     ba.count = c->bin_count;
     ba.diff = c->bin_diff;
-    ba.tile_range = c->tile_range;
+    ba.tile_range = train ? c->tile_range + k * range_stride : c->tile_range;
+    ba.stack_slabs = train;
     ba.tile_order = c->tile_order;
     ba.giant_list = c->giant_list;
     ba.giant_count = c->frame + FW_GIANTS + k;
@@ -643,7 +669,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     GS_MARK(e + 2);
 
     RasterArgs rr{};
-    rr.tile_range = c->tile_range;
+    rr.tile_range = ba.tile_range;
     rr.pair_capacity = c->pair_capacity;
     rr.pair_splat = c->pair_splat;
     rr.record = record;
@@ -661,7 +687,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     rr.tile_done = c->tile_done;
     rr.first = k == 0;
     rr.last = k + 1 == slabs;
-    rr.nproc = train ? c->train_nproc : nullptr;
+    rr.nproc = train ? c->train_nproc + k * pix_stride : nullptr;
     GS_TRY(launch_raster(rr, st));
     GS_MARK(e + 3);
   }
@@ -736,6 +762,9 @@ static gs_status blend_backward(gs_context* c, const gs_train_params* p, const g
     return GS_ERROR_CUDA;
   RasterBackwardArgs rb{};
   rb.tile_range = c->tile_range;
+  rb.range_stride = (u32)range_words(c);
+  rb.slabs = c->train_slabs;
+  rb.nproc_stride = c->max_width * c->max_height;
   rb.pair_capacity = c->pair_capacity;
   rb.pair_splat = c->pair_splat;
   rb.record = c->record;
@@ -959,6 +988,7 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
     gs_context_set_slabs(c->lane[l], c->slab_count, c->slab_end);
     gs_context_set_count_fragments(c->lane[l], c->count_fragments);
     gs_context_set_transmittance_floor(c->lane[l], c->t_floor);
+    gs_context_set_train_slab_min(c->lane[l], c->train_slab_min);
   }
   return GS_SUCCESS;
 }

@@ -11,7 +11,9 @@
 //              footprint box spans more than kGiantPairs tiles are listed as giants and counted by
 //              one CTA each (k_bin_giant_count)
 //   2. scan  : one CTA turns the difference rows into tile counts and an exclusive scan over tiles:
-//              tile t owns pair slots [start_t, start_{t+1}), its cursor starts at start_t
+//              tile t owns pair slots [start_t, start_{t+1}), its cursor starts at start_t (with
+//              stacked slabs -- the differentiable forward keeps every slab's lists for its
+//              backward -- the slots start after the earlier slabs' pairs)
 //   3. emit  : warps expand 32 sorted splats' pairs (span lists, giants by whole CTAs) and append the
 //              splat's sorted position to its tile's segment through the cursor (atomicAdd): each
 //              segment holds the right set of splats in arbitrary order
@@ -291,6 +293,8 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
   __shared__ u32 s_scan[32];
   __shared__ u32 s_len[33];
   const u32 tiles_x = a.tiles_x, rw = tiles_x + 1, T = tiles_x * a.tiles_y;
+  // stacked slabs: this slab's pairs follow the earlier slabs' (read before thread 0 adds this slab's)
+  const u32 base = a.stack_slabs ? (u32)min(*a.pair_sum, (unsigned long long)0xffffffffu) : 0u;
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   for (u32 row = warp; row < a.tiles_y; row += 32) {
     u32 carry = 0;
@@ -317,7 +321,7 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
   u32 s = 0;
   for (u32 t = b; t < e; ++t) s += a.tile_range[2 * t + 1];
   u32 total;
-  u32 run = block_exclusive_scan<1024>(s, s_scan, &total);
+  u32 run = base + block_exclusive_scan<1024>(s, s_scan, &total);
   if (threadIdx.x < 33) s_len[threadIdx.x] = 0;
   __syncthreads();
   for (u32 t = b; t < e; ++t) {
@@ -328,8 +332,8 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
     atomicAdd(&s_len[32 - __clz(c)], 1u);
   }
   if (threadIdx.x == 0) {
-    a.tile_range[2 * T] = total;  // sentinel: end of the last segment
-    a.tile_range[2 * T + 1] = total;
+    a.tile_range[2 * T] = base + total;  // sentinel: end of the last segment
+    a.tile_range[2 * T + 1] = base + total;
   }
   __syncthreads();
   // processing order of the per-tile sort: longest segments first (buckets by bit length)
@@ -347,11 +351,12 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
     a.tile_order[atomicAdd(&s_len[32 - __clz(c)], 1u)] = t;
   }
   if (threadIdx.x == 0) {
+    const u32 need = (u32)min((unsigned long long)base + total, (unsigned long long)0xffffffffu);
     *a.slab_pairs = total;
-    atomicMax(a.pair_total, total);
-    atomicMax(a.pair_peak, total);
+    atomicMax(a.pair_total, need);
+    atomicMax(a.pair_peak, need);
     *a.pair_sum += total;
-    if (total > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
+    if (need > a.pair_capacity) atomicOr(a.err, ERR_CAPACITY);
   }
 }
 

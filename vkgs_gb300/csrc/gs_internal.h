@@ -122,8 +122,9 @@ struct BinArgs {
   u32* pair_key;             // [capacity] sorted position per pair, grouped by tile
   u32* pair_splat;           // [capacity] splat id per pair, grouped by tile, ascending sorted position
   u32 pair_capacity;
+  int stack_slabs;           // pair slots of this slab follow the earlier slabs' (all slabs' lists kept)
   u32* slab_pairs;           // out: pairs this slab needs
-  u32* pair_total;           // out: max over the frame's slabs (atomicMax)
+  u32* pair_total;           // out: max over the frame's slabs of the capacity needed (atomicMax)
   unsigned long long* pair_sum;  // out: sum over the frame's slabs
   u32* pair_peak;            // out: max over every slab since the context was last checked (atomicMax)
   u32* err;
@@ -160,13 +161,16 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
 // (P = dL/do of the pixel, d = pixel - centre) and dL/d(r, g, b); 3 words of padding
 constexpr u32 kGradRec = 12;
 struct RasterBackwardArgs {
-  const u32* tile_range;
+  const u32* tile_range;     // slab k's at tile_range + k * range_stride
+  u32 range_stride;
+  u32 slabs;
   u32 pair_capacity;
   const u32* pair_splat;
   const float4* record;
   u32 width, height, tiles_x, tiles_y;
   const float* state_t;      // final transmittance per pixel
-  const u32* nproc;          // list entries blended per pixel
+  const u32* nproc;          // list entries blended per pixel, slab k's at nproc + k * nproc_stride
+  u32 nproc_stride;
   const float4* grad_rgba;   // dL/d(pixel)
   float* grad_rec;           // [N][kGradRec], accumulated
 };

@@ -260,101 +260,103 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
   const size_t pix = (size_t)py * a.width + px;
   const float fx = __fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f;
   const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
-  const u32 n = inside ? a.nproc[pix] : 0u;
   float Tcur = inside ? a.state_t[pix] : 1.0f;
   const float4 g = inside ? a.grad_rgba[pix] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float S = Tcur * g.w;
-  u32 wmax = n;  // the most list entries any pixel of this warp blended
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
-  if (tid == 0) s_nmax = 0;
-  __syncthreads();
-  if (n) atomicMax(&s_nmax, n);
-  __syncthreads();
-  const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range)[tile];
-  const u32 hi = min(tr.y, a.pair_capacity);
-  const u32 first = hi - min(s_nmax, hi - min(tr.x, a.pair_capacity));  // farthest entry any pixel blended
   const float sx = 2.0f / (float)a.width, sy = 2.0f / (float)a.height;
   const float ox = (float)(2 * tx * kTile + 1) / (float)a.width - 1.0f;
   const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
   const float mx = 0.5f * sx, my = 0.5f * sy;
   const float kExp = -0.5f * 1.4426950408889634f;
-  for (u32 lo = first; lo < hi; lo += kRasterThreads) {  // farthest first: the reverse of the forward
-    const u32 cnt = min((u32)kRasterThreads, hi - lo);
-    u32 mask = 0;
-    if (tid < cnt) {
-      const u32 id = a.pair_splat[lo + tid];
-      const float4* rec = a.record + 4 * (size_t)id;
-      const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
-      s_q0[tid] = q0;
-      s_q1[tid] = q1;
-      s_q2[tid] = rec[2];
-      s_id[tid] = id;
-      mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
-    }
+  for (int slab = (int)a.slabs - 1; slab >= 0; --slab) {  // farthest slab first: the reverse of the forward
+    const u32 n = inside ? a.nproc[(size_t)slab * a.nproc_stride + pix] : 0u;
+    u32 wmax = n;  // the most list entries any pixel of this warp blended
 #pragma unroll
-    for (int b = 0; b < kWarps; ++b) {
-      const u32 bits = __ballot_sync(0xffffffffu, (mask >> b) & 1u);
-      if (lane == 0) s_bits[b][warp] = bits;
-    }
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if (tid == 0) s_nmax = 0;
     __syncthreads();
-    for (int k = 0; k < kWarps; ++k) {
-      u32 word = s_bits[warp][k];
-      while (word) {
-        const u32 j = 32u * k + (u32)(__ffs(word) - 1);
-        word &= word - 1u;
-        const u32 kproc = hi - 1 - (lo + j);  // processing index in the forward (0 = nearest)
-        if (kproc >= wmax) continue;           // behind every pixel of this warp (warp-uniform)
-        const float4 q0 = s_q0[j], q1 = s_q1[j];
-        const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
-        const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
-        const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
-        const bool on = kproc < n && (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
-        float r[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        if (on) {
-          const float4 q2 = s_q2[j];
-          const float G = exp2f(kExp * (u * u + v * v));
-          const float al = q1.w * G;
-          const float inv = __fdividef(1.0f, fmaxf(1.0f - al, 1e-6f));
-          const float Ti = Tcur * inv;
-          const float cg = q2.x * g.x + q2.y * g.y + q2.z * g.z;
-          const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
-          S += (al * cg + al * al * g.w) * Ti;
-          Tcur = Ti;
-          const float P = dLda * G;  // dL/do of this pixel; dL/dq = -o P / 2
-          const float pdx = P * dx, pdy = P * dy;
-          r[0] = P;
-          r[1] = pdx;
-          r[2] = pdy;
-          r[3] = pdx * dx;
-          r[4] = pdy * dy;
-          r[5] = pdx * dy;
-          const float w = al * Ti;
-          r[6] = w * g.x;
-          r[7] = w * g.y;
-          r[8] = w * g.z;
-        }
-        const u32 onmask = __ballot_sync(0xffffffffu, on);
-        if (onmask) {
-          float* dst = a.grad_rec + (size_t)s_id[j] * kGradRec;
-          if (__popc(onmask) <= kDirectLanes) {  // few pixels: their own atomics beat a warp reduction
-            if (on) {
+    if (n) atomicMax(&s_nmax, n);
+    __syncthreads();
+    const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range + (size_t)slab * a.range_stride)[tile];
+    const u32 hi = min(tr.y, a.pair_capacity);
+    const u32 first = hi - min(s_nmax, hi - min(tr.x, a.pair_capacity));  // farthest entry any pixel blended
+    for (u32 lo = first; lo < hi; lo += kRasterThreads) {  // farthest first: the reverse of the forward
+      const u32 cnt = min((u32)kRasterThreads, hi - lo);
+      u32 mask = 0;
+      if (tid < cnt) {
+        const u32 id = a.pair_splat[lo + tid];
+        const float4* rec = a.record + 4 * (size_t)id;
+        const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
+        s_q0[tid] = q0;
+        s_q1[tid] = q1;
+        s_q2[tid] = rec[2];
+        s_id[tid] = id;
+        mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
+      }
 #pragma unroll
-              for (int q = 0; q < 9; ++q) atomicAdd(dst + q, r[q]);
+      for (int b = 0; b < kWarps; ++b) {
+        const u32 bits = __ballot_sync(0xffffffffu, (mask >> b) & 1u);
+        if (lane == 0) s_bits[b][warp] = bits;
+      }
+      __syncthreads();
+      for (int k = 0; k < kWarps; ++k) {
+        u32 word = s_bits[warp][k];
+        while (word) {
+          const u32 j = 32u * k + (u32)(__ffs(word) - 1);
+          word &= word - 1u;
+          const u32 kproc = hi - 1 - (lo + j);  // processing index in the forward (0 = nearest)
+          if (kproc >= wmax) continue;           // behind every pixel of this warp (warp-uniform)
+          const float4 q0 = s_q0[j], q1 = s_q1[j];
+          const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
+          const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
+          const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
+          const bool on = kproc < n && (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
+          float r[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+          if (on) {
+            const float4 q2 = s_q2[j];
+            const float G = exp2f(kExp * (u * u + v * v));
+            const float al = q1.w * G;
+            const float inv = __fdividef(1.0f, fmaxf(1.0f - al, 1e-6f));
+            const float Ti = Tcur * inv;
+            const float cg = q2.x * g.x + q2.y * g.y + q2.z * g.z;
+            const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
+            S += (al * cg + al * al * g.w) * Ti;
+            Tcur = Ti;
+            const float P = dLda * G;  // dL/do of this pixel; dL/dq = -o P / 2
+            const float pdx = P * dx, pdy = P * dy;
+            r[0] = P;
+            r[1] = pdx;
+            r[2] = pdy;
+            r[3] = pdx * dx;
+            r[4] = pdy * dy;
+            r[5] = pdx * dy;
+            const float w = al * Ti;
+            r[6] = w * g.x;
+            r[7] = w * g.y;
+            r[8] = w * g.z;
+          }
+          const u32 onmask = __ballot_sync(0xffffffffu, on);
+          if (onmask) {
+            float* dst = a.grad_rec + (size_t)s_id[j] * kGradRec;
+            if (__popc(onmask) <= kDirectLanes) {  // few pixels: their own atomics beat a warp reduction
+              if (on) {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) atomicAdd(dst + q, r[q]);
+              }
+            } else {
+              float r8;
+              const float sum = warp_sum9(r, &r8);
+              if ((lane & 3u) == 0) {
+                const u32 idx = ((lane >> 4) & 1u) * 4u + ((lane >> 3) & 1u) * 2u + ((lane >> 2) & 1u);
+                atomicAdd(dst + idx, sum);
+              }
+              if (lane == 0) atomicAdd(dst + 8, r8);
             }
-          } else {
-            float r8;
-            const float sum = warp_sum9(r, &r8);
-            if ((lane & 3u) == 0) {
-              const u32 idx = ((lane >> 4) & 1u) * 4u + ((lane >> 3) & 1u) * 2u + ((lane >> 2) & 1u);
-              atomicAdd(dst + idx, sum);
-            }
-            if (lane == 0) atomicAdd(dst + 8, r8);
           }
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
