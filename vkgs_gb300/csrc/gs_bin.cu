@@ -71,13 +71,13 @@ __device__ __forceinline__ void pixel_range(float lo, float hi, u32 size, int& i
   i1 = (int)b;
 }
 
-// Loads the splat's raster record; false when it is not drawn.
+// Loads the splat's centre and axes (the record's first 32 bytes); false when it is not drawn.
 __device__ __forceinline__ bool footprint(const float4* __restrict__ record, u32 id, const TargetGeom& g,
                                           Footprint& f) {
   const float4* r = record + 4 * (size_t)id;
-  const float4 q2 = __ldg(r + 2);
-  if (!(q2.w > 0.0f)) return false;
-  const float4 q0 = __ldg(r + 0), q3 = __ldg(r + 3);
+  const float4 q0 = __ldg(r + REC_CENTER);
+  if (!(q0.x <= 3.0e38f)) return false;  // +inf: not drawn
+  const float4 q3 = __ldg(r + REC_AXES);
   const float cx = q0.x, cy = q0.y;
   const float ax = 3.0f * q3.x, ay = 3.0f * q3.y, bx = 3.0f * q3.z, by = 3.0f * q3.w;
   f.vx[0] = cx - ax - bx, f.vy[0] = cy - ay - by;

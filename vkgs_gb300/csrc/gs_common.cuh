@@ -170,6 +170,15 @@ __device__ __forceinline__ void activate_cov3d(float ls0, float ls1, float ls2, 
 
 __device__ __forceinline__ float activate_opacity(float logit) { return 1.0f / (1.0f + expf(-logit)); }
 
+// Raster record of a splat: 4 float4 at record[4 * id].  The first two slots (32 bytes, one DRAM
+// sector) hold everything the tile binning reads, so its random gathers touch one sector per splat.
+enum : u32 {
+  REC_CENTER = 0,  // (cx, cy, m00, m01): NDC centre (cx = +inf when the splat is not drawn), row 0 of M
+  REC_AXES = 1,    // rot_scale columns (a.x, a.y, b.x, b.y): the 3-sigma quad is c +- 3a +- 3b
+  REC_ROW1 = 2,    // (m10, m11, z, opacity): row 1 of M = rot_scale^-1, NDC depth, opacity
+  REC_COLOR = 3,   // (r, g, b, drawn)
+};
+
 struct FrameConst {
   float pvm[16];    // projection * view * model, glm operand order (rank.comp:32)
   float model[16];

@@ -164,10 +164,10 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
   const bool drawn = (s1 > 0.0f) && isfinite(m00) && isfinite(m01) && isfinite(m10) && isfinite(m11) &&
                      (nz >= 0.0f) && (nz < 1.0f);
   float4* rec = a.record + 4 * (size_t)id;
-  rec[0] = make_float4(nx, ny, m00, m01);
-  rec[1] = make_float4(m10, m11, nz, o);
-  rec[2] = make_float4(fminf(color[0], 1.0f), fminf(color[1], 1.0f), fminf(color[2], 1.0f), drawn ? 1.0f : 0.0f);
-  rec[3] = make_float4(rs0, rs1, rs2, rs3);
+  rec[REC_CENTER] = make_float4(drawn ? nx : INFINITY, ny, m00, m01);  // +inf: the binning skips it
+  rec[REC_AXES] = make_float4(rs0, rs1, rs2, rs3);
+  rec[REC_ROW1] = make_float4(m10, m11, nz, o);
+  rec[REC_COLOR] = make_float4(fminf(color[0], 1.0f), fminf(color[1], 1.0f), fminf(color[2], 1.0f), drawn ? 1.0f : 0.0f);
   if (a.inst_by_id) {
     float4* inst = reinterpret_cast<float4*>(a.inst_by_id + 12 * (size_t)id);
     inst[0] = make_float4(nx, ny, nz, 0.0f);

@@ -104,10 +104,10 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
     if (tid < cnt) {
       const u32 id = a.pair_splat[hi - 1 - tid];  // nearest first
       const float4* rec = a.record + 4 * (size_t)id;
-      const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
+      const float4 q0 = rec[REC_CENTER], q1 = rec[REC_ROW1], q3 = rec[REC_AXES];
       s_q0[tid] = q0;
       s_q1[tid] = q1;
-      s_q2[tid] = rec[2];
+      s_q2[tid] = rec[REC_COLOR];
       mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
     }
 #pragma unroll
@@ -286,10 +286,10 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
       if (tid < cnt) {
         const u32 id = a.pair_splat[lo + tid];
         const float4* rec = a.record + 4 * (size_t)id;
-        const float4 q0 = rec[0], q1 = rec[1], q3 = rec[3];
+        const float4 q0 = rec[REC_CENTER], q1 = rec[REC_ROW1], q3 = rec[REC_AXES];
         s_q0[tid] = q0;
         s_q1[tid] = q1;
-        s_q2[tid] = rec[2];
+        s_q2[tid] = rec[REC_COLOR];
         s_id[tid] = id;
         mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
       }
