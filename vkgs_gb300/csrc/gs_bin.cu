@@ -287,15 +287,38 @@ __global__ __launch_bounds__(kGiantThreads) void k_bin_giant_count(const BinArgs
   }
 }
 
-// 2. tile counts -> segments.  One CTA: warps turn difference rows into counts (and clear them),
-//    then an exclusive scan over the tiles in row-major order sets each tile's start and cursor.
+// Warp-aggregated slot in bucket b (< 64) of s_len: lanes with equal buckets (6 ballots) share one
+// shared-memory atomic; returns the lane's slot.  Whole warp.
+__device__ __forceinline__ u32 bucket_slot(u32* s_len, u32 b, bool valid) {
+  const u32 lane = threadIdx.x & 31u;
+  u32 peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const bool bit = (b >> k) & 1u;
+    const u32 bb = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  const int leader = valid ? __ffs(peers) - 1 : 0;
+  u32 old = 0;
+  if (valid && (int)lane == leader) old = atomicAdd(&s_len[b], (u32)__popc(peers));
+  old = __shfl_sync(0xffffffffu, old, leader);
+  return old + __popc(peers & lanemask_lt());
+}
+
+// 2. tile counts -> segments.  One CTA: warps turn difference rows into counts (and clear them; the
+//    counts stay in shared memory when they fit), then an exclusive scan over the tiles in row-major
+//    order sets each tile's start and cursor, and the tiles are listed longest segment first.
+constexpr u32 kScanSmemTiles = 10240;
 __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
   __shared__ u32 s_scan[32];
   __shared__ u32 s_len[33];
+  __shared__ u32 s_cnt[kScanSmemTiles];
   const u32 tiles_x = a.tiles_x, rw = tiles_x + 1, T = tiles_x * a.tiles_y;
   // stacked slabs: this slab's pairs follow the earlier slabs' (read before thread 0 adds this slab's)
   const u32 base = a.stack_slabs ? (u32)min(*a.pair_sum, (unsigned long long)0xffffffffu) : 0u;
+  u32* cnt = T <= kScanSmemTiles ? s_cnt : a.tile_order;  // tile_order is rewritten last
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  if (threadIdx.x < 33) s_len[threadIdx.x] = 0;
   for (u32 row = warp; row < a.tiles_y; row += 32) {
     u32 carry = 0;
     for (u32 c0 = 0; c0 < rw; c0 += 32) {
@@ -311,7 +334,7 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
         const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (u32)o) incl += y;
       }
-      if (c < tiles_x) a.tile_range[2 * (row * tiles_x + c) + 1] = carry + incl;
+      if (c < tiles_x) cnt[row * tiles_x + c] = carry + incl;
       carry += __shfl_sync(0xffffffffu, incl, 31);
     }
   }
@@ -319,17 +342,19 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
   const u32 per = (T + 1023) / 1024;
   const u32 b = min(threadIdx.x * per, T), e = min(b + per, T);
   u32 s = 0;
-  for (u32 t = b; t < e; ++t) s += a.tile_range[2 * t + 1];
+  for (u32 t = b; t < e; ++t) s += cnt[t];
   u32 total;
   u32 run = base + block_exclusive_scan<1024>(s, s_scan, &total);
-  if (threadIdx.x < 33) s_len[threadIdx.x] = 0;
-  __syncthreads();
-  for (u32 t = b; t < e; ++t) {
-    const u32 c = a.tile_range[2 * t + 1];
-    a.tile_range[2 * t] = run;
-    a.tile_range[2 * t + 1] = run;
-    run += c;
-    atomicAdd(&s_len[32 - __clz(c)], 1u);
+  for (u32 i = 0; i < per; ++i) {  // warp-uniform trip count
+    const u32 t = b + i;
+    const bool valid = t < e;
+    const u32 c = valid ? cnt[t] : 0u;
+    if (valid) {
+      a.tile_range[2 * t] = run;
+      a.tile_range[2 * t + 1] = run;
+      run += c;
+    }
+    bucket_slot(s_len, 32 - __clz(c), valid);
   }
   if (threadIdx.x == 0) {
     a.tile_range[2 * T] = base + total;  // sentinel: end of the last segment
@@ -346,9 +371,12 @@ __global__ __launch_bounds__(1024) void k_bin_scan(const BinArgs a) {
     }
   }
   __syncthreads();
-  for (u32 t = b; t < e; ++t) {
-    const u32 c = a.tile_range[2 * t + 2] - a.tile_range[2 * t];
-    a.tile_order[atomicAdd(&s_len[32 - __clz(c)], 1u)] = t;
+  for (u32 i = 0; i < per; ++i) {
+    const u32 t = b + i;
+    const bool valid = t < e;
+    const u32 c = valid ? a.tile_range[2 * t + 2] - a.tile_range[2 * t] : 0u;
+    const u32 slot = bucket_slot(s_len, 32 - __clz(c), valid);
+    if (valid) a.tile_order[slot] = t;
   }
   if (threadIdx.x == 0) {
     const u32 need = (u32)min((unsigned long long)base + total, (unsigned long long)0xffffffffu);
