@@ -286,6 +286,24 @@ gs_status gs_viewer_create(gs_viewer** viewer, gs_context* context, const gs_spl
 gs_status gs_viewer_frame(gs_viewer* viewer, const gs_camera* camera, gs_stream stream);
 void gs_viewer_destroy(gs_viewer* viewer);
 
+/* Frames in flight, as the reference's viewer keeps them (two, engine.cc:743): the viewer owns
+ * frames_in_flight slots (1 ... GS_MAX_FRAMES_IN_FLIGHT), each a captured frame with its own scratch
+ * (slot 0 uses `context`, the others own contexts with its capacities and settings), its own stream and
+ * its own target (targets[slot]).  gs_viewer_submit puts the next frame into the next slot in turn:
+ * it starts after the work enqueued on `stream` so far (and after that slot's previous frame) and does
+ * not hold `stream` back, so consecutive frames overlap on the GPU; *slot receives the slot.
+ * gs_viewer_wait makes `stream` wait for that slot's latest frame (e.g. before reading its target);
+ * a slot's target must not be written by the next frame of that slot before the caller is done with it,
+ * which holds when the caller's reads are enqueued on `stream` before the submit that reuses the slot.
+ * gs_viewer_frame = submit + wait.  gs_viewer_check waits for every slot on `stream`, synchronises and
+ * returns the first device error of the slots' contexts. */
+#define GS_MAX_FRAMES_IN_FLIGHT 4
+gs_status gs_viewer_create_frames(gs_viewer** viewer, gs_context* context, const gs_splats* splats,
+                                  const gs_camera* camera, const gs_target* targets, uint32_t frames_in_flight);
+gs_status gs_viewer_submit(gs_viewer* viewer, const gs_camera* camera, gs_stream stream, uint32_t* slot);
+gs_status gs_viewer_wait(gs_viewer* viewer, uint32_t slot, gs_stream stream);
+gs_status gs_viewer_check(gs_viewer* viewer, gs_stream stream);
+
 /* The differentiable path over many views of the same splats (no counterpart in the reference): view v
  * is drawn by render lane v (gs_context_set_batch_lanes; n_views may not exceed the lanes,
  * GS_ERROR_CAPACITY otherwise), which keeps that view's forward state; the activation runs once.  The

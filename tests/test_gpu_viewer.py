@@ -43,3 +43,47 @@ def test_viewer_rejects_other_resolution(cuda):
     with pytest.raises(GsError):
         v.frame(Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=640, height=360)))
     v.close()
+
+
+@pytest.mark.parametrize("inflight", [2, 3])
+def test_viewer_frames_in_flight_equal_direct_renders(cuda, inflight):
+    """Frames submitted without waiting (one slot per frame in flight, own scratch and stream each) are
+    the direct renders; a slot's target is read back before the slot is reused."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer, Viewer, parse_ply
+
+    rows = syn.splat_rows(300_000, 23, "shell")
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    cams = [Camera.from_spec(s) for s in syn.circle_cameras(width=640, height=360)]
+    direct = Renderer(300_000, 640, 360)
+    want = [direct.render_checked(splats, c)[0].clone() for c in cams]
+    r = Renderer(300_000, 640, 360)
+    for c in cams:
+        r.render_checked(splats, c)
+    v = Viewer(r, splats, cams[0], torch.zeros((360, 640, 4), device="cuda"), frames_in_flight=inflight)
+    main = torch.cuda.current_stream()
+    got = []
+    for k in range(2 * len(cams)):
+        slot = v.submit(cams[k % len(cams)])
+        v.wait(slot)  # the copy below is ordered after this frame, and before the slot's next submit
+        got.append(v.colors[slot].clone())
+        if k == 0:
+            assert len(set(id(c) for c in v.colors)) == inflight
+    v.check()
+    main.synchronize()
+    for k, img in enumerate(got):
+        assert torch.equal(img, want[k % len(cams)]), k
+    v.close()
+
+
+def test_viewer_frames_in_flight_rejects_bad_counts(cuda):
+    import torch
+    from vkgs_gb300 import Camera, GsError, Renderer, Viewer, parse_ply
+
+    rows = syn.splat_rows(1000, 24)
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=320, height=180))
+    r = Renderer(1000, 320, 180)
+    for n in (0, 5):
+        with pytest.raises((GsError, ValueError)):
+            Viewer(r, splats, cam, [torch.zeros((180, 320, 4), device="cuda")] * max(n, 1), frames_in_flight=n)

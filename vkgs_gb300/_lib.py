@@ -23,6 +23,7 @@ GS_NUM_STAGES = 6
 GS_SORT_NOALLOC_MAX_COUNT = 1 << 20  # include/vkgs_gb300.h
 GS_MAX_SLABS = 4
 GS_MAX_LANES = 32
+GS_MAX_FRAMES_IN_FLIGHT = 4
 STAGES = ("cull_project", "depth_sort", "bin", "emit", "tile_sort", "raster")
 
 
@@ -90,6 +91,11 @@ SIGNATURES = [
     ("gs_viewer_create", c_int, [POINTER(c_void_p), c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget)]),
     ("gs_viewer_frame", c_int, [c_void_p, POINTER(GsCamera), c_void_p]),
     ("gs_viewer_destroy", None, [c_void_p]),
+    ("gs_viewer_create_frames", c_int,
+     [POINTER(c_void_p), c_void_p, POINTER(GsSplats), POINTER(GsCamera), POINTER(GsTarget), c_uint32]),
+    ("gs_viewer_submit", c_int, [c_void_p, POINTER(GsCamera), c_void_p, POINTER(c_uint32)]),
+    ("gs_viewer_wait", c_int, [c_void_p, c_uint32, c_void_p]),
+    ("gs_viewer_check", c_int, [c_void_p, c_void_p]),
     ("gs_context_set_batch_shared_cull", c_int, [c_void_p, c_int]),
     ("gs_render_batched", c_int,
      [c_void_p, POINTER(GsSplats), c_uint32, POINTER(GsCamera), POINTER(GsTarget), c_void_p]),

@@ -329,26 +329,55 @@ class Renderer:
 class Viewer:
     """The viewer's per-frame loop as a CUDA graph (gs_viewer_*): one captured frame of `renderer` drawing
     `splats` into `color`; frame(camera) updates the camera inside the graph and launches it.  The
-    renderer must not render anything else while the viewer exists."""
+    renderer must not render anything else while the viewer exists.
 
-    def __init__(self, renderer: Renderer, splats: Splats, camera: Camera, color: torch.Tensor):
-        _need_cuda(color, "color", torch.float32)
-        if tuple(color.shape) != (int(camera.height), int(camera.width), 4):
-            raise ValueError("color must be (H, W, 4)")
+    frames_in_flight > 1 (the reference viewer keeps two): one captured frame per slot, each with its own
+    scratch, stream and target (`color` may then be a list of targets, else they are allocated);
+    submit(camera) starts the next frame without waiting for the previous ones and returns its slot,
+    wait(slot) orders the current stream after that slot's latest frame, check() after all of them."""
+
+    def __init__(self, renderer: Renderer, splats: Splats, camera: Camera, color, frames_in_flight: int = 1):
+        n = int(frames_in_flight)
+        shape = (int(camera.height), int(camera.width), 4)
+        if isinstance(color, (list, tuple)):
+            colors = list(color)
+        else:
+            colors = [color] + [torch.empty_like(color) for _ in range(n - 1)]
+        if len(colors) != n:
+            raise ValueError("one colour target per frame in flight")
+        for c in colors:
+            _need_cuda(c, "color", torch.float32)
+            if tuple(c.shape) != shape:
+                raise ValueError("color must be (H, W, 4)")
         self._lib = renderer._lib
-        self.renderer, self.splats, self.color = renderer, splats, color  # keep the buffers alive
+        self.renderer, self.splats, self.colors = renderer, splats, colors  # keep the buffers alive
+        self.color = colors[0]
         self._s = splats.struct()
         cam = camera.struct()
-        target = L.GsTarget(_ptr(color), None, None)
+        targets = (L.GsTarget * n)(*[L.GsTarget(_ptr(c), None, None) for c in colors])
         h = ctypes.c_void_p()
-        _check(self._lib.gs_viewer_create(ctypes.byref(h), renderer._h, ctypes.byref(self._s), ctypes.byref(cam),
-                                          ctypes.byref(target)), "gs_viewer_create")
+        _check(self._lib.gs_viewer_create_frames(ctypes.byref(h), renderer._h, ctypes.byref(self._s),
+                                                 ctypes.byref(cam), targets, n), "gs_viewer_create_frames")
         self._h = h
 
     def frame(self, camera: Camera, stream=None) -> torch.Tensor:
+        """Renders the next frame, ordered on `stream`; returns its target."""
+        slot = self.submit(camera, stream)
+        self.wait(slot, stream)
+        return self.colors[slot]
+
+    def submit(self, camera: Camera, stream=None) -> int:
         cam = camera.struct()
-        _check(self._lib.gs_viewer_frame(self._h, ctypes.byref(cam), _stream(stream)), "gs_viewer_frame")
-        return self.color
+        slot = ctypes.c_uint32()
+        _check(self._lib.gs_viewer_submit(self._h, ctypes.byref(cam), _stream(stream), ctypes.byref(slot)),
+               "gs_viewer_submit")
+        return int(slot.value)
+
+    def wait(self, slot: int, stream=None) -> None:
+        _check(self._lib.gs_viewer_wait(self._h, int(slot), _stream(stream)), "gs_viewer_wait")
+
+    def check(self, stream=None) -> None:
+        _check(self._lib.gs_viewer_check(self._h, _stream(stream)), "gs_viewer_check")
 
     def close(self) -> None:
         if getattr(self, "_h", None):

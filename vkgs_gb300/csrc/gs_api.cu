@@ -892,33 +892,77 @@ gs_status gs_train_backward_batched(gs_context* c, const gs_train_params* p, uin
 
 // ------------------------------------------------------------------ viewer loop (CUDA graph per frame)
 
-struct gs_viewer {
+// One captured frame of the viewer: its context (the caller's for slot 0, an own one otherwise), the
+// graph and the cull node whose camera constants are rewritten per frame.
+struct ViewerSlot {
   gs_context* ctx = nullptr;
-  cudaStream_t capture = nullptr;
+  bool own_ctx = false;
+  cudaStream_t stream = nullptr;  // capture stream; with frames in flight also the slot's launch stream
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaGraphNode_t cull = nullptr;  // kernel node whose FrameConst is rewritten per frame
+  cudaGraphNode_t cull = nullptr;
   CullArgs cull_args{};
   cudaKernelNodeParams cull_params{};
+  cudaEvent_t done = nullptr;
+};
+
+struct gs_viewer {
+  u32 nslots = 0;
+  ViewerSlot slot[GS_MAX_FRAMES_IN_FLIGHT];
+  cudaEvent_t fork = nullptr;
+  u32 next = 0;  // slot of the next frame
   u32 width = 0, height = 0, count = 0;
 };
 
 void gs_viewer_destroy(gs_viewer* v) {
   if (!v) return;
-  if (v->exec) cudaGraphExecDestroy(v->exec);
-  if (v->graph) cudaGraphDestroy(v->graph);
-  if (v->capture) cudaStreamDestroy(v->capture);
+  if (v->nslots > 1) cudaDeviceSynchronize();
+  for (u32 i = 0; i < v->nslots; ++i) {
+    ViewerSlot& sl = v->slot[i];
+    if (sl.exec) cudaGraphExecDestroy(sl.exec);
+    if (sl.graph) cudaGraphDestroy(sl.graph);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.own_ctx) gs_context_destroy(sl.ctx);
+  }
+  if (v->fork) cudaEventDestroy(v->fork);
   delete v;
 }
 
-gs_status gs_viewer_create(gs_viewer** out, gs_context* c, const gs_splats* s, const gs_camera* cam,
-                           const gs_target* t) {
-  if (!out || !c || !s || !cam || !t) return GS_ERROR_INVALID_ARGUMENT;
+static gs_status capture_slot(ViewerSlot& sl, const gs_splats* s, const gs_camera* cam, const gs_target* t) {
+  if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess) return GS_ERROR_CUDA;
+  if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) return GS_ERROR_CUDA;
+  if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GS_ERROR_CUDA;
+  const gs_status r = gs_render(sl.ctx, s, cam, t, nullptr, reinterpret_cast<gs_stream>(sl.stream));
+  const cudaError_t e = cudaStreamEndCapture(sl.stream, &sl.graph);
+  if (r != GS_SUCCESS) return r;
+  if (e != cudaSuccess) return GS_ERROR_CUDA;
+  size_t count = 0;
+  if (cudaGraphGetNodes(sl.graph, nullptr, &count) != cudaSuccess) return GS_ERROR_CUDA;
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (count && cudaGraphGetNodes(sl.graph, nodes.data(), &count) != cudaSuccess) return GS_ERROR_CUDA;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType type;
+    if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp{};
+    if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) continue;
+    if (kp.func != cull_project_kernel()) continue;
+    sl.cull = node;
+    sl.cull_params = kp;
+    sl.cull_args = *reinterpret_cast<const CullArgs*>(kp.kernelParams[1]);
+  }
+  if (s->count && !sl.cull) return GS_ERROR_INTERNAL;
+  if (cudaGraphInstantiate(&sl.exec, sl.graph, 0) != cudaSuccess) return GS_ERROR_CUDA;
+  return GS_SUCCESS;
+}
+
+gs_status gs_viewer_create_frames(gs_viewer** out, gs_context* c, const gs_splats* s, const gs_camera* cam,
+                                  const gs_target* targets, uint32_t frames_in_flight) {
+  if (!out || !c || !s || !cam || !targets) return GS_ERROR_INVALID_ARGUMENT;
   *out = nullptr;
-  if (c->timing) return GS_ERROR_INVALID_ARGUMENT;
+  if (frames_in_flight == 0 || frames_in_flight > GS_MAX_FRAMES_IN_FLIGHT || c->timing) return GS_ERROR_INVALID_ARGUMENT;
   gs_viewer* v = new (std::nothrow) gs_viewer();
   if (!v) return GS_ERROR_OUT_OF_MEMORY;
-  v->ctx = c;
   v->width = cam->width;
   v->height = cam->height;
   v->count = s->count;
@@ -926,46 +970,83 @@ gs_status gs_viewer_create(gs_viewer** out, gs_context* c, const gs_splats* s, c
     gs_viewer_destroy(v);
     return st;
   };
-  if (cudaStreamCreateWithFlags(&v->capture, cudaStreamNonBlocking) != cudaSuccess) return fail(GS_ERROR_CUDA);
-  if (cudaStreamBeginCapture(v->capture, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fail(GS_ERROR_CUDA);
-  const gs_status r = gs_render(c, s, cam, t, nullptr, reinterpret_cast<gs_stream>(v->capture));
-  const cudaError_t e = cudaStreamEndCapture(v->capture, &v->graph);
-  if (r != GS_SUCCESS) return fail(r);
-  if (e != cudaSuccess) return fail(GS_ERROR_CUDA);
-  size_t count = 0;
-  if (cudaGraphGetNodes(v->graph, nullptr, &count) != cudaSuccess) return fail(GS_ERROR_CUDA);
-  std::vector<cudaGraphNode_t> nodes(count);
-  if (count && cudaGraphGetNodes(v->graph, nodes.data(), &count) != cudaSuccess) return fail(GS_ERROR_CUDA);
-  for (cudaGraphNode_t node : nodes) {
-    cudaGraphNodeType type;
-    if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
-    cudaKernelNodeParams kp{};
-    if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) continue;
-    if (kp.func != cull_project_kernel()) continue;
-    v->cull = node;
-    v->cull_params = kp;
-    v->cull_args = *reinterpret_cast<const CullArgs*>(kp.kernelParams[1]);
+  if (cudaEventCreateWithFlags(&v->fork, cudaEventDisableTiming) != cudaSuccess) return fail(GS_ERROR_CUDA);
+  gs_context_options o{c->max_splats, c->max_width, c->max_height, c->pair_capacity};
+  for (u32 i = 0; i < frames_in_flight; ++i) {
+    ViewerSlot& sl = v->slot[i];
+    v->nslots = i + 1;  // what exists so far is torn down on failure
+    if (i == 0) {
+      sl.ctx = c;
+    } else {  // an own context with the caller's settings
+      gs_status st = gs_context_create(&sl.ctx, &o);
+      if (st != GS_SUCCESS) return fail(st);
+      sl.own_ctx = true;
+      gs_context_set_slabs(sl.ctx, c->slab_count, c->slab_end);
+      gs_context_set_count_fragments(sl.ctx, c->count_fragments);
+      gs_context_set_transmittance_floor(sl.ctx, c->t_floor);
+    }
+    const gs_status st = capture_slot(sl, s, cam, &targets[i]);
+    if (st != GS_SUCCESS) return fail(st);
   }
-  if (s->count && !v->cull) return fail(GS_ERROR_INTERNAL);
-  if (cudaGraphInstantiate(&v->exec, v->graph, 0) != cudaSuccess) return fail(GS_ERROR_CUDA);
   *out = v;
   return GS_SUCCESS;
 }
 
-gs_status gs_viewer_frame(gs_viewer* v, const gs_camera* cam, gs_stream stream) {
+gs_status gs_viewer_create(gs_viewer** out, gs_context* c, const gs_splats* s, const gs_camera* cam,
+                           const gs_target* t) {
+  return gs_viewer_create_frames(out, c, s, cam, t, 1);
+}
+
+gs_status gs_viewer_submit(gs_viewer* v, const gs_camera* cam, gs_stream stream, uint32_t* slot_out) {
   if (!v || !cam) return GS_ERROR_INVALID_ARGUMENT;
   if (cam->width != v->width || cam->height != v->height) return GS_ERROR_INVALID_ARGUMENT;
-  if (v->cull) {
+  const u32 i = v->next;
+  ViewerSlot& sl = v->slot[i];
+  if (sl.cull) {  // later launches of the graph see the new camera; launches in flight keep theirs
     FrameConst fc;
     frame_constants(cam->projection, cam->view, cam->model, cam->camera_position, v->width, v->height, v->count, &fc);
-    CullArgs ca = v->cull_args;
+    CullArgs ca = sl.cull_args;
     void* args[2] = {&fc, &ca};
-    cudaKernelNodeParams kp = v->cull_params;
+    cudaKernelNodeParams kp = sl.cull_params;
     kp.kernelParams = args;
     kp.extra = nullptr;
-    if (cudaGraphExecKernelNodeSetParams(v->exec, v->cull, &kp) != cudaSuccess) return GS_ERROR_CUDA;
+    if (cudaGraphExecKernelNodeSetParams(sl.exec, sl.cull, &kp) != cudaSuccess) return GS_ERROR_CUDA;
   }
-  return from_cuda(cudaGraphLaunch(v->exec, reinterpret_cast<cudaStream_t>(stream)));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (v->nslots == 1) {  // one slot: the frame runs on the caller's stream
+    if (cudaGraphLaunch(sl.exec, st) != cudaSuccess || cudaEventRecord(sl.done, st) != cudaSuccess)
+      return GS_ERROR_CUDA;
+  } else {  // after the caller's prior work, on the slot's stream (its previous frame precedes it there)
+    if (cudaEventRecord(v->fork, st) != cudaSuccess || cudaStreamWaitEvent(sl.stream, v->fork, 0) != cudaSuccess ||
+        cudaGraphLaunch(sl.exec, sl.stream) != cudaSuccess || cudaEventRecord(sl.done, sl.stream) != cudaSuccess)
+      return GS_ERROR_CUDA;
+  }
+  if (slot_out) *slot_out = i;
+  v->next = (i + 1) % v->nslots;
+  return GS_SUCCESS;
+}
+
+gs_status gs_viewer_wait(gs_viewer* v, uint32_t slot, gs_stream stream) {
+  if (!v || slot >= v->nslots) return GS_ERROR_INVALID_ARGUMENT;
+  return from_cuda(cudaStreamWaitEvent(reinterpret_cast<cudaStream_t>(stream), v->slot[slot].done, 0));
+}
+
+gs_status gs_viewer_frame(gs_viewer* v, const gs_camera* cam, gs_stream stream) {
+  u32 slot = 0;
+  const gs_status r = gs_viewer_submit(v, cam, stream, &slot);
+  if (r != GS_SUCCESS || v->nslots == 1) return r;
+  return gs_viewer_wait(v, slot, stream);
+}
+
+gs_status gs_viewer_check(gs_viewer* v, gs_stream stream) {
+  if (!v) return GS_ERROR_INVALID_ARGUMENT;
+  gs_status worst = GS_SUCCESS;
+  for (u32 i = 0; i < v->nslots; ++i) {
+    if (gs_viewer_wait(v, i, stream) != GS_SUCCESS) return GS_ERROR_CUDA;
+    const gs_status r = gs_context_check(v->slot[i].ctx, stream, nullptr);
+    if (r != GS_SUCCESS && worst == GS_SUCCESS) worst = r;
+  }
+  return worst;
 }
 
 gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
