@@ -64,7 +64,9 @@ def test_viewer_frames_in_flight_equal_direct_renders(cuda, inflight):
     main = torch.cuda.current_stream()
     got = []
     for k in range(2 * len(cams)):
+        assert v.next_slot == k % inflight
         slot = v.submit(cams[k % len(cams)])
+        assert slot == k % inflight
         v.wait(slot)  # the copy below is ordered after this frame, and before the slot's next submit
         got.append(v.colors[slot].clone())
         if k == 0:

@@ -359,6 +359,7 @@ class Viewer:
         _check(self._lib.gs_viewer_create_frames(ctypes.byref(h), renderer._h, ctypes.byref(self._s),
                                                  ctypes.byref(cam), targets, n), "gs_viewer_create_frames")
         self._h = h
+        self._next = 0
 
     def frame(self, camera: Camera, stream=None) -> torch.Tensor:
         """Renders the next frame, ordered on `stream`; returns its target."""
@@ -371,7 +372,13 @@ class Viewer:
         slot = ctypes.c_uint32()
         _check(self._lib.gs_viewer_submit(self._h, ctypes.byref(cam), _stream(stream), ctypes.byref(slot)),
                "gs_viewer_submit")
+        self._next = (int(slot.value) + 1) % len(self.colors)
         return int(slot.value)
+
+    @property
+    def next_slot(self) -> int:
+        """The slot the next submit will use (slots are used in turn)."""
+        return self._next
 
     def wait(self, slot: int, stream=None) -> None:
         _check(self._lib.gs_viewer_wait(self._h, int(slot), _stream(stream)), "gs_viewer_wait")
