@@ -297,7 +297,7 @@ void gs_viewer_destroy(gs_viewer* viewer);
  * which holds when the caller's reads are enqueued on `stream` before the submit that reuses the slot.
  * gs_viewer_frame = submit + wait.  gs_viewer_check waits for every slot on `stream`, synchronises and
  * returns the first device error of the slots' contexts. */
-#define GS_MAX_FRAMES_IN_FLIGHT 4
+#define GS_MAX_FRAMES_IN_FLIGHT 8
 gs_status gs_viewer_create_frames(gs_viewer** viewer, gs_context* context, const gs_splats* splats,
                                   const gs_camera* camera, const gs_target* targets, uint32_t frames_in_flight);
 gs_status gs_viewer_submit(gs_viewer* viewer, const gs_camera* camera, gs_stream stream, uint32_t* slot);

@@ -86,6 +86,6 @@ def test_viewer_frames_in_flight_rejects_bad_counts(cuda):
     splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
     cam = Camera.from_spec(syn.CameraSpec(eye=(0.0, 0.0, 6.0), width=320, height=180))
     r = Renderer(1000, 320, 180)
-    for n in (0, 5):
+    for n in (0, 9):
         with pytest.raises((GsError, ValueError)):
             Viewer(r, splats, cam, [torch.zeros((180, 320, 4), device="cuda")] * max(n, 1), frames_in_flight=n)

@@ -23,7 +23,7 @@ GS_NUM_STAGES = 6
 GS_SORT_NOALLOC_MAX_COUNT = 1 << 20  # include/vkgs_gb300.h
 GS_MAX_SLABS = 4
 GS_MAX_LANES = 32
-GS_MAX_FRAMES_IN_FLIGHT = 4
+GS_MAX_FRAMES_IN_FLIGHT = 8
 STAGES = ("cull_project", "depth_sort", "bin", "emit", "tile_sort", "raster")
 
 
