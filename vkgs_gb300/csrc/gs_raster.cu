@@ -239,7 +239,7 @@ __device__ __forceinline__ float warp_sum9(float v[9], float* v8) {
   return t;
 }
 
-constexpr u32 kDirectLanes = 4;  // a record covering at most this many pixels of a warp skips the reduction
+constexpr u32 kDirectLanes = 8;  // a record covering at most this many pixels of a warp skips the reduction
 
 // Each warp (an 8x4 pixel block) walks only the records that can touch its block, reduces the 9
 // per-splat values over its 32 pixels (warp_sum9) and adds them with one atomic per value; a record
