@@ -130,14 +130,14 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic():
-    """dram bytes per raster launch from the committed ncu summary, if one exists."""
+def raster_profile() -> dict:
+    """The raster's figures from the committed ncu summary (DRAM bytes per launch, issue utilisation)."""
     path = os.path.join(ROOT, "profiles", "raster_large.json")
     try:
         with open(path) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            return json.load(f)
     except (OSError, ValueError):
-        return None
+        return {}
 
 
 def make_scene(n_override=None):
@@ -618,7 +618,9 @@ def run_ours(args):
                         "each frame copied to pinned host memory; a copy overlaps the following frames"},
         "gpu_launches": None,
         "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "T lane-ops/s", "frac": achieved / fp32_peak, "traffic": profile_traffic(),
+                     "unit": "T lane-ops/s", "frac": achieved / fp32_peak,
+                     "traffic": raster_profile().get("dram_bytes_per_launch"),
+                     "issue_active_ncu": raster_profile().get("issue_active"),
                      "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
                      "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair met front to "
                              "back while the pixel's transmittance is >= the transmittance floor (1e-4)"},
