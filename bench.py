@@ -5,12 +5,13 @@ Workload ("large"): 6,000,000 synthetic 3D Gaussians (70 % on a radius-4 shell, 
 [-10,10]^3, seed 1), 1600x900, nine cameras (eight on a radius-8 circle + one zoomed out at radius
 20), FP32 with binary16 SH.  A step is one full frame -- cull + depth key + compaction + projection
 + SH, depth sort, per-slab tile binning, per-tile sort, tile raster + blend -- for camera
-(step mod 9), issued through the viewer loop (gs_viewer_frame: the frame captured once as a CUDA
-graph, the camera rewritten inside it every step); the same frames issued as one gs_render call each
-are reported beside it with their per-stage times.  Inputs (816 MB of splat buffers) are resident in
-HBM and larger than L2, so no L2 flush is interposed.  The line also carries the batched form (64
-views of a 1M-splat scene in one graph vs the per-view loop) and the differentiable form (fwd+bwd
-it/s, 200k splats at 800x800).
+(step mod 9), issued through the viewer loop with frames in flight (gs_viewer_submit: one captured
+CUDA graph per slot, the camera rewritten inside it every step, consecutive frames overlapping; the
+reference's viewer keeps two frames in flight); one frame in flight and one gs_render call per step
+are reported beside it, the latter with per-stage times.  Inputs (816 MB of splat buffers) are
+resident in HBM and larger than L2, so no L2 flush is interposed.  The line also carries the batched
+form (64 views of a 1M-splat scene in one graph vs the per-view loop), the differentiable form
+(fwd+bwd it/s, 200k splats at 800x800) and the batched differentiation (3M splats, 16 views/step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
