@@ -100,7 +100,8 @@ def test_train_rejects_bad_shapes(cuda):
         train.render(p, cam, r)
 
 
-def test_batched_gradients_equal_sum_of_views(cuda, oracle):
+@pytest.mark.parametrize("shared", [True, False])
+def test_batched_gradients_equal_sum_of_views(cuda, oracle, shared):
     """The batched differentiable path draws each view exactly as the one-view path and its gradients are
     the per-view gradients summed (atomic accumulation: equal up to FP32 summation order)."""
     import torch
@@ -128,6 +129,7 @@ def test_batched_gradients_equal_sum_of_views(cuda, oracle):
     r = Renderer(n, 200, 160)
     r.set_batch_lanes(len(cams))
     r.set_train_slab_min(0)  # stacked depth slabs on the lanes; the one-view reference uses one slab
+    r.set_batch_shared_cull(shared)  # one cull pass for all views, or one per lane
     params = _gpu_params(rows)
     imgs = train.render_batched(params, cams, r)
     sum((img * wt).sum() for img, wt in zip(imgs, weights)).backward()

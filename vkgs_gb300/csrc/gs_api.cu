@@ -98,6 +98,7 @@ struct gs_context {
   float* train_opacity = nullptr;
   u32* train_nproc = nullptr;      // per slab and pixel: list entries blended
   u32 train_slabs = 1;             // depth slabs of the last differentiable forward
+  const float4* train_record = nullptr;  // the records that forward drew (its backward reads them)
   // The differentiable forward uses the slab schedule from this many splats on; below it the per-slab
   // fixed cost (seven more launches, the blended-count clears) outweighs the pairs it saves (measured:
   // 200k splats at 800x800, one slab 0.86 ms per fwd+bwd step vs 0.94 ms with two; 3M splats x 16
@@ -632,6 +633,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   const size_t pix_stride = (size_t)c->max_width * c->max_height;
   if (train) {
     c->train_slabs = slabs;
+    c->train_record = record;
     for (u32 k = 1; k < slabs; ++k)  // tiles finished earlier are skipped by later slabs: count 0
       GS_TRY(cudaMemsetAsync(c->train_nproc + k * pix_stride, 0, (size_t)W * H * sizeof(u32), st));
   }
@@ -767,7 +769,7 @@ static gs_status blend_backward(gs_context* c, const gs_train_params* p, const g
   rb.nproc_stride = c->max_width * c->max_height;
   rb.pair_capacity = c->pair_capacity;
   rb.pair_splat = c->pair_splat;
-  rb.record = c->record;
+  rb.record = c->train_record ? c->train_record : c->record;
   rb.width = W;
   rb.height = H;
   rb.tiles_x = (W + kTile - 1) / kTile;
@@ -835,6 +837,120 @@ static gs_status join_lanes(gs_context* c, u32 used, cudaStream_t st) {
   return GS_SUCCESS;
 }
 
+// Per-view cull outputs of the batched forms, for up to kMaxBatchViews views of up to max_splats
+// splats: [visible words][tickets][look-back status of every view] (cleared per batch), then per view
+// its compacted keys, ids and records.  Allocated by the first batched call that needs them (never
+// while the stream is being captured: that call takes the per-lane cull instead).
+constexpr u32 kMaxBatchViews = 64;
+
+struct BatchLayout {
+  size_t status_off, head_bytes, status_words, view_stride, key_off, index_off, record_off, total;
+};
+
+static BatchLayout batch_layout(u32 views, u32 n) {
+  BatchLayout b{};
+  const auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  b.status_words = (n + kCullTile - 1) / kCullTile;
+  b.status_off = up((size_t)(kMaxBatchViews + kMaxBatchViews / kMaxCullViews + 1) * sizeof(u32));
+  b.head_bytes = b.status_off + up((size_t)views * b.status_words * sizeof(u64));
+  b.key_off = 0;
+  b.index_off = up((size_t)n * sizeof(u32));
+  b.record_off = b.index_off + up((size_t)n * sizeof(u32));
+  b.view_stride = b.record_off + up((size_t)n * 4 * sizeof(float4));
+  b.total = b.head_bytes + (size_t)views * b.view_stride;
+  return b;
+}
+
+static bool batch_buffers(gs_context* c, u32 views, cudaStream_t st) {
+  if (c->batch_arena && views <= c->batch_views && c->max_splats <= c->batch_n) return true;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return false;
+  free_batch_buffers(c);
+  const BatchLayout b = batch_layout(views, c->max_splats);
+  if (cudaMalloc(&c->batch_arena, b.total) != cudaSuccess) {
+    cudaGetLastError();
+    c->batch_arena = nullptr;
+    return false;
+  }
+  c->batch_bytes = b.total;
+  c->batch_views = views;
+  c->batch_n = c->max_splats;
+  return true;
+}
+
+// The arena's buffers of slot w.
+static PreCulled batch_slot(const gs_context* c, u32 w) {
+  const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
+  char* vb = c->batch_arena + b.head_bytes + (size_t)w * b.view_stride;
+  return PreCulled{reinterpret_cast<u32*>(vb + b.key_off), reinterpret_cast<u32*>(vb + b.index_off),
+                   reinterpret_cast<float4*>(vb + b.record_off), reinterpret_cast<u32*>(c->batch_arena) + w};
+}
+
+// The cull + projection of cams[0 .. nv) (nv <= batch_views) into arena slots 0 .. nv-1, k_cull_views
+// launches of up to kMaxCullViews views on `st`.  sh32: FP32 SH (the differentiable path).
+static gs_status shared_cull(gs_context* c, const gs_splats* s, const float* sh32, u32 nv, const gs_camera* cams,
+                             cudaStream_t st) {
+  const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
+  char* base = c->batch_arena;
+  u32* tickets = reinterpret_cast<u32*>(base) + kMaxBatchViews;
+  u64* status = reinterpret_cast<u64*>(base + b.status_off);
+  if (cudaMemsetAsync(base, 0, b.head_bytes, st) != cudaSuccess) return GS_ERROR_CUDA;
+  std::unique_ptr<CullViewsArgs> ca(new CullViewsArgs{});
+  for (u32 c0 = 0; c0 < nv; c0 += kMaxCullViews) {
+    const u32 cnt = std::min(kMaxCullViews, nv - c0);
+    ca->position = s->position;
+    ca->cov3d = s->cov3d;
+    ca->opacity = s->opacity;
+    ca->sh = s->sh;
+    ca->sh32 = sh32;
+    ca->n = s->count;
+    ca->count = cnt;
+    ca->ticket = tickets + c0 / kMaxCullViews;
+    ca->epoch = 1;
+    ca->err = c->err;
+    ca->num_sms = c->num_sms;
+    for (u32 i = 0; i < cnt; ++i) {
+      const u32 w = c0 + i;
+      const gs_camera& cam = cams[w];
+      frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, s->count,
+                      &ca->fc[i]);
+      const PreCulled pre = batch_slot(c, w);
+      ca->view[i] = CullView{pre.key, pre.index, pre.record, pre.visible, status + (size_t)w * b.status_words};
+    }
+    if (launch_cull_views(*ca, st) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  return GS_SUCCESS;
+}
+
+// Views [v0, v0 + nv) of the batch: their culls in k_cull_views launches on `st`, then their frames
+// from the depth sort on, spread over the lanes.
+static gs_status batched_group(gs_context* c, const gs_splats* s, u32 v0, u32 nv, const gs_camera* cams,
+                               const gs_target* targets, cudaStream_t st) {
+  gs_status r = shared_cull(c, s, nullptr, nv, cams + v0, st);
+  if (r != GS_SUCCESS) return r;
+  const u32 used = std::min(c->nlanes, std::max(nv, 1u));
+  if ((r = fork_lanes(c, used, st)) != GS_SUCCESS) return r;
+  // Largest views first, each to the lane with the least work so far (work ~ pixels + a fixed cost per
+  // view), so the lanes finish together.
+  std::vector<u32> order(nv);
+  for (u32 w = 0; w < nv; ++w) order[w] = w;
+  const auto work = [&](u32 w) { return (double)cams[v0 + w].width * cams[v0 + w].height + 250000.0; };
+  std::stable_sort(order.begin(), order.end(), [&](u32 x, u32 y) { return work(x) > work(y); });
+  double load[GS_MAX_LANES] = {};
+  for (u32 w : order) {
+    u32 l = 0;
+    for (u32 k = 1; k < used; ++k)
+      if (load[k] < load[l]) l = k;
+    load[l] += work(w);
+    const PreCulled pre = batch_slot(c, w);
+    r = render_frame(c->lane[l], s, nullptr, &cams[v0 + w], &targets[v0 + w], nullptr,
+                     reinterpret_cast<gs_stream>(c->lane_stream[l]), &pre);
+    if (r != GS_SUCCESS) return r;
+  }
+  return join_lanes(c, used, st);
+}
+
+
 gs_status gs_train_forward_batched(gs_context* c, const gs_train_params* p, uint32_t n_views, const gs_camera* cams,
                                    float* const* colors, gs_stream stream) {
   if (!c || (n_views && (!cams || !colors))) return GS_ERROR_INVALID_ARGUMENT;
@@ -857,12 +973,18 @@ gs_status gs_train_forward_batched(gs_context* c, const gs_train_params* p, uint
   ta.cov3d = c->train_cov;
   ta.opacity = c->train_opacity;
   if (launch_activate(ta, st) != cudaSuccess) return GS_ERROR_CUDA;
-  gs_status r = fork_lanes(c, n_views, st);
-  if (r != GS_SUCCESS) return r;
   const gs_splats s{c->train_pos, c->train_cov, c->train_opacity, nullptr, p->count};
+  // one shared cull + projection pass for all views when its buffers are available (each lane then
+  // starts at the depth sort and keeps pointing at its view's records for the backward)
+  const bool shared = p->count > 0 && c->multi_view_cull && batch_buffers(c, n_views, st);
+  gs_status r = shared ? shared_cull(c, &s, p->sh, n_views, cams, st) : GS_SUCCESS;
+  if (r != GS_SUCCESS) return r;
+  if ((r = fork_lanes(c, n_views, st)) != GS_SUCCESS) return r;
   for (u32 v = 0; v < n_views; ++v) {
     gs_target t{colors[v], nullptr, nullptr};
-    r = render_frame(c->lane[v], &s, p->sh, &cams[v], &t, nullptr, reinterpret_cast<gs_stream>(c->lane_stream[v]));
+    const PreCulled pre = shared ? batch_slot(c, v) : PreCulled{};
+    r = render_frame(c->lane[v], &s, p->sh, &cams[v], &t, nullptr, reinterpret_cast<gs_stream>(c->lane_stream[v]),
+                     shared ? &pre : nullptr);
     if (r != GS_SUCCESS) return r;
   }
   c->last_batched = true;
@@ -1072,107 +1194,6 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
     gs_context_set_train_slab_min(c->lane[l], c->train_slab_min);
   }
   return GS_SUCCESS;
-}
-
-// Per-view cull outputs of the batched form, for up to kMaxBatchViews views of up to max_splats splats:
-// [visible words][tickets][look-back status of every view] (cleared per batch), then per view its
-// compacted keys, ids and records.  Allocated by the first batched call that needs them (never while
-// the stream is being captured: that call takes the per-lane cull instead).
-constexpr u32 kMaxBatchViews = 64;
-
-struct BatchLayout {
-  size_t status_off, head_bytes, status_words, view_stride, key_off, index_off, record_off, total;
-};
-
-static BatchLayout batch_layout(u32 views, u32 n) {
-  BatchLayout b{};
-  const auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  b.status_words = (n + kCullTile - 1) / kCullTile;
-  b.status_off = up((size_t)(kMaxBatchViews + kMaxBatchViews / kMaxCullViews + 1) * sizeof(u32));
-  b.head_bytes = b.status_off + up((size_t)views * b.status_words * sizeof(u64));
-  b.key_off = 0;
-  b.index_off = up((size_t)n * sizeof(u32));
-  b.record_off = b.index_off + up((size_t)n * sizeof(u32));
-  b.view_stride = b.record_off + up((size_t)n * 4 * sizeof(float4));
-  b.total = b.head_bytes + (size_t)views * b.view_stride;
-  return b;
-}
-
-static bool batch_buffers(gs_context* c, u32 views, cudaStream_t st) {
-  if (c->batch_arena && views <= c->batch_views && c->max_splats <= c->batch_n) return true;
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return false;
-  free_batch_buffers(c);
-  const BatchLayout b = batch_layout(views, c->max_splats);
-  if (cudaMalloc(&c->batch_arena, b.total) != cudaSuccess) {
-    cudaGetLastError();
-    c->batch_arena = nullptr;
-    return false;
-  }
-  c->batch_bytes = b.total;
-  c->batch_views = views;
-  c->batch_n = c->max_splats;
-  return true;
-}
-
-// Views [v0, v0 + nv) of the batch: their culls in k_cull_views launches on `st`, then their frames
-// from the depth sort on, spread over the lanes.
-static gs_status batched_group(gs_context* c, const gs_splats* s, u32 v0, u32 nv, const gs_camera* cams,
-                               const gs_target* targets, cudaStream_t st) {
-  const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
-  char* base = c->batch_arena;
-  u32* visible = reinterpret_cast<u32*>(base);
-  u32* tickets = visible + kMaxBatchViews;
-  u64* status = reinterpret_cast<u64*>(base + b.status_off);
-  char* views = base + b.head_bytes;
-  if (cudaMemsetAsync(base, 0, b.head_bytes, st) != cudaSuccess) return GS_ERROR_CUDA;
-  std::unique_ptr<CullViewsArgs> ca(new CullViewsArgs{});
-  for (u32 c0 = 0; c0 < nv; c0 += kMaxCullViews) {
-    const u32 cnt = std::min(kMaxCullViews, nv - c0);
-    ca->position = s->position;
-    ca->cov3d = s->cov3d;
-    ca->opacity = s->opacity;
-    ca->sh = s->sh;
-    ca->n = s->count;
-    ca->count = cnt;
-    ca->ticket = tickets + c0 / kMaxCullViews;
-    ca->epoch = 1;
-    ca->err = c->err;
-    ca->num_sms = c->num_sms;
-    for (u32 i = 0; i < cnt; ++i) {
-      const u32 w = c0 + i;  // slot in the arena
-      const gs_camera& cam = cams[v0 + w];
-      frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, s->count,
-                      &ca->fc[i]);
-      char* vb = views + (size_t)w * b.view_stride;
-      ca->view[i] = CullView{reinterpret_cast<u32*>(vb + b.key_off), reinterpret_cast<u32*>(vb + b.index_off),
-                             reinterpret_cast<float4*>(vb + b.record_off), visible + w, status + (size_t)w * b.status_words};
-    }
-    if (launch_cull_views(*ca, st) != cudaSuccess) return GS_ERROR_CUDA;
-  }
-  const u32 used = std::min(c->nlanes, std::max(nv, 1u));
-  gs_status r = fork_lanes(c, used, st);
-  if (r != GS_SUCCESS) return r;
-  // Largest views first, each to the lane with the least work so far (work ~ pixels + a fixed cost per
-  // view), so the lanes finish together.
-  std::vector<u32> order(nv);
-  for (u32 w = 0; w < nv; ++w) order[w] = w;
-  const auto work = [&](u32 w) { return (double)cams[v0 + w].width * cams[v0 + w].height + 250000.0; };
-  std::stable_sort(order.begin(), order.end(), [&](u32 x, u32 y) { return work(x) > work(y); });
-  double load[GS_MAX_LANES] = {};
-  for (u32 w : order) {
-    u32 l = 0;
-    for (u32 k = 1; k < used; ++k)
-      if (load[k] < load[l]) l = k;
-    load[l] += work(w);
-    char* vb = views + (size_t)w * b.view_stride;
-    const PreCulled pre{reinterpret_cast<u32*>(vb + b.key_off), reinterpret_cast<u32*>(vb + b.index_off),
-                        reinterpret_cast<float4*>(vb + b.record_off), visible + w};
-    r = render_frame(c->lane[l], s, nullptr, &cams[v0 + w], &targets[v0 + w], nullptr,
-                     reinterpret_cast<gs_stream>(c->lane_stream[l]), &pre);
-    if (r != GS_SUCCESS) return r;
-  }
-  return join_lanes(c, used, st);
 }
 
 gs_status gs_context_set_batch_shared_cull(gs_context* c, int enable) {

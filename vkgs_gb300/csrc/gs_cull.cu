@@ -259,7 +259,8 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
 // and later resolves view v's look-back, each visible (splat, view) is projected into that view's
 // records, and then keyed into its compacted lists.
 // The splat's covariance, opacity and SH are read once per partition from DRAM and then from cache for
-// the other views.  Outputs are bit-identical to k_cull_project<false> run per view.
+// the other views.  Outputs are bit-identical to k_cull_project<SH32> run per view.
+template <bool SH32>
 __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs a) {
   __shared__ u32 s_cnt[kMaxCullViews][kCullItems][kCullThreads / 32];
   __shared__ u32 s_base[kMaxCullViews], s_acc[kMaxCullViews];
@@ -273,6 +274,7 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs
   ca.cov3d = a.cov3d;
   ca.opacity = a.opacity;
   ca.sh = a.sh;
+  ca.sh32 = a.sh32;
   for (;;) {
     if (tid == 0) s_part = atomicAdd(a.ticket, 1u);
     __syncthreads();
@@ -328,7 +330,7 @@ __global__ __launch_bounds__(kCullThreads) void k_cull_views(const CullViewsArgs
       for (u32 v = 0; v < nv; ++v) {  // the same view across the warp: no divergence between views
         if ((visbits[k] >> v) & 1u) {
           ca.record = a.view[v].record;
-          project_splat<false>(a.fc[v], ca, id, px[k], py[k], pz[k]);
+          project_splat<SH32>(a.fc[v], ca, id, px[k], py[k], pz[k]);
         }
       }
     }
@@ -365,7 +367,10 @@ cudaError_t launch_cull_views(const CullViewsArgs& a, cudaStream_t stream) {
   if (a.count > kMaxCullViews) return cudaErrorInvalidValue;
   const u32 parts = (a.n + kCullTile - 1) / kCullTile;
   const int sms = a.num_sms > 0 ? a.num_sms : 1;
-  k_cull_views<<<min(parts, (u32)sms * 8u), kCullThreads, 0, stream>>>(a);
+  if (a.sh32)
+    k_cull_views<true><<<min(parts, (u32)sms * 8u), kCullThreads, 0, stream>>>(a);
+  else
+    k_cull_views<false><<<min(parts, (u32)sms * 8u), kCullThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -61,7 +61,7 @@ struct CullArgs {
 };
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
 
-// The cull + projection of up to kMaxCullViews views of the same splats in one launch (binary16 SH).
+// The cull + projection of up to kMaxCullViews views of the same splats in one launch.
 constexpr u32 kMaxCullViews = 32;
 struct CullView {
   u32* key;            // compacted keys / ids of the view, ascending id
@@ -75,6 +75,7 @@ struct CullViewsArgs {
   const float* cov3d;
   const float* opacity;
   const uint16_t* sh;
+  const float* sh32;  // non-null: FP32 SH instead of sh (the differentiable path)
   u32 n;
   u32 count;  // views
   u32* ticket;
