@@ -16,7 +16,7 @@ from dataclasses import dataclass
 
 import torch
 
-LANES = (1, 2, 4, 8, 12, 16)
+LANES = (1, 2, 4, 8, 12, 16, 24, 32)
 SLABS = ((1024,), (128, 1024), (256, 1024))
 
 
