@@ -61,6 +61,23 @@ def test_null_arguments_are_rejected_without_a_device(lib):
     assert lib.gs_parse_ply(None, 0, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_context_reserve(None, None) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_context_set_count_fragments(None, 1) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_slabs(None, 0, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_transmittance_floor(None, 1e-4) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_batch_lanes(None, 0) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_batch_shared_cull(None, 1) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_train_slab_min(None, 0) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_render_batched(None, None, 0, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_train_forward(None, None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_train_backward(None, None, None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_train_forward_batched(None, None, 0, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_train_backward_batched(None, None, 0, None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_create(None, None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_create_frames(None, None, None, None, None, 2) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_frame(None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_submit(None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_wait(None, 0, None) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_viewer_check(None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    lib.gs_viewer_destroy(None)
     lib.gs_context_destroy(None)
     lib.gs_sorter_destroy(None)
 
