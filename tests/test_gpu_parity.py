@@ -91,6 +91,15 @@ def test_ragged_sizes(cuda, oracle, n, w, h, seed):
     assert_parity(render_gpu(act, c), render_cpu(oracle, act, c))
 
 
+@pytest.mark.parametrize("w,h", [(2560, 1440), (3840, 2160)])
+def test_high_resolution_parity(cuda, oracle, w, h):
+    """More tiles than the scan keeps in shared memory (14400 and 32400 > 10240): the scan's global path."""
+    rows = syn.splat_rows(60_000, 17, "shell")
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (2.0, 1.0, 7.0), width=w, height=h)
+    assert_parity(render_gpu(act, c), render_cpu(oracle, act, c))
+
+
 def test_empty_scene(cuda, oracle):
     act = (np.zeros((0, 3), np.float32), np.zeros((0, 6), np.float32), np.zeros(0, np.float32),
            np.zeros((0, 48), np.uint16))
