@@ -105,6 +105,35 @@ def test_batched_graph_capture_replays(cuda):
     r.check()
 
 
+def test_batched_first_call_under_capture_uses_per_lane_cull(cuda):
+    """A batched call captured before the shared cull's buffers exist cannot allocate them: it falls back
+    to one cull per lane, and the captured batch still renders the same images."""
+    import torch
+    from vkgs_gb300 import Renderer
+
+    _, splats, specs, cams, colors = _setup(100_000, 16, 5, 508)
+    ref = Renderer(100_000, 1920, 1080)
+    want = [ref.render_checked(splats, c)[0].clone() for c in cams]
+    r = Renderer(100_000, 1920, 1080)
+    for c in cams:  # size the pair capacity (single-view renders allocate nothing for the batch)
+        r.render_checked(splats, c)
+    r.set_batch_lanes(3)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        r.render_batched(splats, cams, colors)
+    for _ in range(2):
+        for c in colors:
+            c.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip(colors, want):
+            assert torch.equal(a, b)
+    r.check()
+
+
 def test_batched_capacity_overflow_recovers(cuda):
     import torch
     from vkgs_gb300 import GsError, Renderer
