@@ -219,3 +219,17 @@ def test_depth_input_culls_fragments_behind_it(oracle):
     np.testing.assert_array_equal(same["image"], full["image"])
     zero = oracle.render_frame(pos, cov, opa, sh, cam, depth_in=np.zeros((90, 160), np.float32))
     assert zero["fragments"] == 0
+
+
+def test_fp32_vs_fp64_report_runs(oracle, capsys, monkeypatch):
+    """The per-workload FP32-vs-FP64 report (oracle/fp32_vs_fp64.py) on the small gradient-check workload."""
+    import json
+    import sys
+
+    from oracle import fp32_vs_fp64
+
+    monkeypatch.setattr(sys, "argv", ["fp32_vs_fp64", "--workloads", "grad_check", "--cameras", "1"])
+    assert fp32_vs_fp64.main() == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["workload"] == "grad_check" and line["visible"] > 0
+    assert line["max_abs"] < 0.05 and line["pixels_over_1_255"] < 0.01
