@@ -171,6 +171,11 @@ typedef struct gs_frame_stats {
 
 /* Creates a context on the current CUDA device and reserves all scratch for the given capacities. */
 gs_status gs_context_create(gs_context** context, const gs_context_options* options);
+
+/* The device bytes gs_context_create allocates for these options (the reference preallocates its
+ * storage the same way, engine.cc:483-521), computed on the host without a device.  Render lanes,
+ * frames in flight and the batched form's per-view buffers allocate on top of it. */
+gs_status gs_context_scratch_bytes(const gs_context_options* options, size_t* bytes);
 void gs_context_destroy(gs_context* context);
 
 /* Grows the reserved scratch (never shrinks).  Synchronises the device; not for use inside capture. */

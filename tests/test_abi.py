@@ -82,6 +82,22 @@ def test_null_arguments_are_rejected_without_a_device(lib):
     lib.gs_sorter_destroy(None)
 
 
+def test_scratch_bytes_without_a_device(lib):
+    def need(n, w, h, pairs=0):
+        b = ctypes.c_size_t()
+        assert lib.gs_context_scratch_bytes(ctypes.byref(L.GsContextOptions(n, w, h, pairs)), ctypes.byref(b)) == 0
+        return b.value
+
+    small, big = need(100_000, 1600, 900), need(6_000_000, 1600, 900)
+    assert big > small > 100_000 * 64              # at least the 64-byte raster record per splat
+    assert need(6_000_000, 3840, 2160) > big          # per-pixel state grows with the target
+    assert need(6_000_000, 1600, 900, 1 << 20) < big  # fewer tile pairs than the default 16 per splat
+    assert lib.gs_context_scratch_bytes(None, None) == L.GS_ERROR_INVALID_ARGUMENT
+    b = ctypes.c_size_t()
+    assert lib.gs_context_scratch_bytes(ctypes.byref(L.GsContextOptions(10, 0, 0, 0)), ctypes.byref(b)) == \
+        L.GS_ERROR_INVALID_ARGUMENT
+
+
 def test_camera_helpers_match_oracle_bits(lib, oracle):
     from vkgs_gb300 import api
 

@@ -85,6 +85,7 @@ SIGNATURES = [
     ("gs_context_destroy", None, [c_void_p]),
     ("gs_context_reserve", c_int, [c_void_p, POINTER(GsContextOptions)]),
     ("gs_context_set_count_fragments", c_int, [c_void_p, c_int]),
+    ("gs_context_scratch_bytes", c_int, [POINTER(GsContextOptions), POINTER(c_size_t)]),
     ("gs_context_set_slabs", c_int, [c_void_p, c_uint32, POINTER(c_uint32)]),
     ("gs_context_set_transmittance_floor", c_int, [c_void_p, c_float]),
     ("gs_context_set_batch_lanes", c_int, [c_void_p, c_uint32]),

@@ -139,14 +139,14 @@ struct gs_sorter {
   u32* err = nullptr;  // device word
 };
 
-static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, u32 max_height, u32 max_pairs) {
+// The context arena: every per-frame buffer at the given capacities, carved from one allocation (cv
+// with a null base only measures).
+static void context_layout(Carver& cv, gs_context* t, u32 max_splats, u32 max_width, u32 max_height, u32 max_pairs) {
   const u32 tiles_x = (max_width + kTile - 1) / kTile, tiles_y = (max_height + kTile - 1) / kTile;
   const u32 max_tiles = std::max(1u, tiles_x * tiles_y);
   const u32 n = std::max(1u, max_splats);
   const u32 pairs = std::max(1u, max_pairs);
-  if (max_tiles > kMaxTiles) return GS_ERROR_CAPACITY;
-  Carver plan;
-  auto layout = [&](Carver& cv, gs_context* t) {
+  {
     t->frame = cv.take<u32>(FW_WORDS);
     t->err = cv.take<u32>(4);
     t->key = cv.take<u32>(n);
@@ -176,9 +176,18 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
     t->radix_status_words = radix_status_words(n);
     t->radix_status = cv.take<u64>(t->radix_status_words);
     t->status_bytes_end = cv.offset;
-  };
+  }
+}
+
+static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, u32 max_height, u32 max_pairs) {
+  const u32 tiles_x = (max_width + kTile - 1) / kTile, tiles_y = (max_height + kTile - 1) / kTile;
+  const u32 max_tiles = std::max(1u, tiles_x * tiles_y);
+  const u32 n = std::max(1u, max_splats);
+  const u32 pairs = std::max(1u, max_pairs);
+  if (max_tiles > kMaxTiles) return GS_ERROR_CAPACITY;
+  Carver plan;
   gs_context probe;
-  layout(plan, &probe);
+  context_layout(plan, &probe, max_splats, max_width, max_height, max_pairs);
   char* arena = nullptr;
   if (cudaMalloc(&arena, plan.offset) != cudaSuccess) {
     cudaGetLastError();
@@ -194,7 +203,7 @@ static gs_status context_allocate(gs_context* c, u32 max_splats, u32 max_width, 
   }
   Carver real;
   real.base = arena;
-  layout(real, c);
+  context_layout(real, c, max_splats, max_width, max_height, max_pairs);
   c->arena = arena;
   c->arena_bytes = plan.offset;
   c->max_splats = n;
@@ -374,6 +383,21 @@ gs_status gs_sorter_check(gs_sorter* s, gs_stream stream) {
 
 // ------------------------------------------------------------------ context
 
+static u32 default_pairs(const gs_context_options* o) {
+  return o->max_tile_pairs ? o->max_tile_pairs : (u32)std::min<uint64_t>(16ull * o->max_splats, 0x3fffffffull);
+}
+
+gs_status gs_context_scratch_bytes(const gs_context_options* o, size_t* bytes) {
+  if (!o || !bytes || o->max_width == 0 || o->max_height == 0) return GS_ERROR_INVALID_ARGUMENT;
+  const u32 tiles_x = (o->max_width + kTile - 1) / kTile, tiles_y = (o->max_height + kTile - 1) / kTile;
+  if ((uint64_t)tiles_x * tiles_y > kMaxTiles) return GS_ERROR_CAPACITY;
+  Carver plan;
+  gs_context probe;
+  context_layout(plan, &probe, o->max_splats, o->max_width, o->max_height, default_pairs(o));
+  *bytes = plan.offset;
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_create(gs_context** out, const gs_context_options* o) {
   if (!out || !o) return GS_ERROR_INVALID_ARGUMENT;
   *out = nullptr;
@@ -385,8 +409,7 @@ gs_status gs_context_create(gs_context** out, const gs_context_options* o) {
     delete c;
     return GS_ERROR_CUDA;
   }
-  const u32 pairs = o->max_tile_pairs ? o->max_tile_pairs : (u32)std::min<uint64_t>(16ull * o->max_splats, 0x3fffffffull);
-  const gs_status st = context_allocate(c, o->max_splats, o->max_width, o->max_height, pairs);
+  const gs_status st = context_allocate(c, o->max_splats, o->max_width, o->max_height, default_pairs(o));
   if (st != GS_SUCCESS) {
     delete c;
     return st;
