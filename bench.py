@@ -498,9 +498,18 @@ def run_ours(args):
         viewer.check(main)
         return e0.elapsed_time(e1)
 
-    # One frame in flight, for comparison: each frame waits for the previous one.
+    # One frame in flight, for comparison: each frame waits for the previous one.  An event after every
+    # frame gives the per-frame latency distribution (median, p10, p90).
     viewer = Viewer(r, splats, cams[0], color)
-    single_ms = viewer_rate(viewer, lambda k: viewer.frame(cams[k % len(cams)], stream=main), K)
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+
+    def one_frame(k):  # (warm-up frames record too; the timed frames record again afterwards)
+        viewer.frame(cams[k % len(cams)], stream=main)
+        if k < K:
+            marks[k].record(main)
+
+    single_ms = viewer_rate(viewer, one_frame, K)
+    frame_ms = [e0.elapsed_time(marks[0])] + [marks[k - 1].elapsed_time(marks[k]) for k in range(1, K)]
     viewer.close()
 
     # The headline: FRAMES_IN_FLIGHT frames in flight (the reference's viewer keeps two in flight).
@@ -638,6 +647,7 @@ def run_ours(args):
                 "one captured CUDA graph per slot, the camera constants rewritten in its cull node every step, "
                 "each slot with its own scratch, stream and target, consecutive frames overlapping",
         "one_frame_in_flight": {"frames_per_s": world * K / (single_ms / 1e3), "ms_per_frame": single_ms / K,
+                                "frame_ms_p10_median_p90": [float(np.percentile(frame_ms, q)) for q in (10, 50, 90)],
                                 "form": "gs_viewer_frame: each frame waits for the previous one"},
         "direct_render": {"frames_per_s": world / (direct_ms / 1e3), "ms_per_frame": direct_ms,
                           "form": "one gs_render call per step (stages_ms are measured on this path)"},
