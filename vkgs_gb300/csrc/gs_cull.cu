@@ -9,8 +9,10 @@
 //      0<=z<=1, key = floatBitsToUint(1 - z);
 //   2. the reference's atomicAdd slot becomes an order-preserving compaction (ballot counts per warp,
 //      a bounded decoupled look-back across partitions), so equal keys later sort by ascending id;
+//      the partition publishes its count at once and resolves its own offset only after step 3;
 //   3. projection.comp:80-179 for every visible splat, written at record[id] (raster record) and,
-//      if requested, inst_by_id[id] (the reference's 48-byte instance layout).
+//      if requested, inst_by_id[id] (the reference's 48-byte instance layout);
+//   4. the keys and ids are written at their compacted slots.
 // The reference's inverse-index pass (inverse_index.comp) has no counterpart: records are keyed by
 // splat id and the later stages gather them through the sorted index list.
 #include <cuda_fp16.h>
