@@ -98,6 +98,14 @@ def test_scratch_bytes_without_a_device(lib):
         L.GS_ERROR_INVALID_ARGUMENT
 
 
+def test_python_scratch_bytes_matches_the_abi(lib):
+    import vkgs_gb300
+
+    b = ctypes.c_size_t()
+    assert lib.gs_context_scratch_bytes(ctypes.byref(L.GsContextOptions(1000, 64, 64, 0)), ctypes.byref(b)) == 0
+    assert vkgs_gb300.scratch_bytes(1000, 64, 64) == b.value
+
+
 def test_camera_helpers_match_oracle_bits(lib, oracle):
     from vkgs_gb300 import api
 

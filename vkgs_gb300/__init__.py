@@ -5,7 +5,7 @@ for PyTorch callers.  See ``vkgs_gb300.api`` for the tensor-level calls.
 """
 
 from .api import (Camera, GsError, Renderer, Sorter, Splats, Viewer, load, look_at, orbit_eye, parse_ply,
-                  perspective, ply_header, write_ply)
+                  perspective, ply_header, scratch_bytes, write_ply)
 
 __all__ = ["Camera", "GsError", "Renderer", "Sorter", "Splats", "Viewer", "load", "look_at", "orbit_eye",
-           "parse_ply", "perspective", "ply_header", "write_ply"]
+           "parse_ply", "perspective", "ply_header", "scratch_bytes", "write_ply"]

@@ -159,6 +159,14 @@ class Camera:
 
 # ----------------------------------------------------------------------------------------- renderer
 
+def scratch_bytes(max_splats: int, max_width: int, max_height: int, max_tile_pairs: int = 0) -> int:
+    """Device bytes a Renderer with these capacities allocates (gs_context_scratch_bytes; no device needed)."""
+    opts = L.GsContextOptions(int(max_splats), int(max_width), int(max_height), int(max_tile_pairs))
+    b = ctypes.c_size_t()
+    _check(L.load().gs_context_scratch_bytes(ctypes.byref(opts), ctypes.byref(b)), "gs_context_scratch_bytes")
+    return int(b.value)
+
+
 class Renderer:
     """A render context (gs_context): reserved scratch for up to max_splats at max_width x max_height."""
 
