@@ -73,3 +73,22 @@ def test_gradient_allreduce_and_view_partition_two_ranks():
         views = out[rank]["views"]
         assert sorted(v for s in views for v in s) == list(range(16))
         assert views[0] and views[1] and not set(views[0]) & set(views[1])
+
+
+def test_render_batched_sharded_renders_exactly_the_ranks_views():
+    class _Renderer:
+        def __init__(self):
+            self.got = None
+
+        def render_batched(self, splats, cams, colors):
+            self.got = (list(cams), list(colors))
+
+    cams = [_Cam(*syn.RESOLUTIONS[i % len(syn.RESOLUTIONS)]) for i in range(10)]
+    colors = [f"target{i}" for i in range(10)]
+    seen = []
+    for rank in range(3):
+        r = _Renderer()
+        mine = shard.render_batched_sharded(r, None, cams, colors, rank, 3)
+        assert r.got == ([cams[v] for v in mine], [colors[v] for v in mine])
+        seen += mine
+    assert sorted(seen) == list(range(10))
