@@ -385,6 +385,12 @@ def run_reference(args):
     cpu_frames(oracle, act, cams, args.cpu_band_stride, max(args.warmup, 0), threads)
     times = cpu_frames(oracle, act, cams, args.cpu_band_stride, args.steps, threads)
     value = len(times) / sum(times)
+    # the same restatement on one core: one camera, a sparser band sample
+    oracle.set_num_threads(1)
+    try:
+        one = cpu_frames(oracle, act, cams, 4 * args.cpu_band_stride, 1, 1)
+    finally:
+        oracle.set_num_threads(threads)
     sample = (f"per step: full cull/key/sort/projection of all {n} splats + blend of every "
               f"{args.cpu_band_stride}th 16-row band, blend time x{args.cpu_band_stride}")
     line = {
@@ -393,7 +399,11 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{WORKLOAD}: {n} splats, 1600x900, 9 cameras (8 on r=8 circle + r=20)",
                    "l2": "inputs (816 MB) exceed L2"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "one_core": {"value": 1.0 / one[0], "unit": UNIT, "cores": 1,
+                                      "sample": f"camera 0: full cull/key/sort/projection + blend of 1 in "
+                                                f"{4 * args.cpu_band_stride} 16-row bands, blend time x"
+                                                f"{4 * args.cpu_band_stride}"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's Vulkan shaders cannot run here (no graphics stack); this arm is the scalar "
                 "C restatement of those shaders (oracle/cpu_ref.c) on all host cores",
