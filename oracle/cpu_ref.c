@@ -4,9 +4,16 @@
  * TEST INFRASTRUCTURE ONLY: used by tests/, the smoke check and the CPU-baseline
  * arm of bench.py as the checker.  The product never links or calls it.
  *
- * Parity status: UNPINNED (the reference ships no tests, fixtures or runnable
- * CPU code; its shaders need a Vulkan stack that does not exist here).  This is
- * a scalar restatement of the reference shaders; each function cites the
+ * Parity status: PINNED to the reference's own shaders.  The reference ships no
+ * tests, fixtures or CPU code, and its shaders need a Vulkan stack that does
+ * not exist here, so oracle/glsl/ compiles the shader bodies themselves for the
+ * host (a C++ GLSL subset + a harness that dispatches them in the engine's
+ * order and rasterises the quads with Vulkan's rules); tests/test_ref_pin.py
+ * compares this file with them (live where the reference checkout exists,
+ * through tests/golden/ref_fixtures.json everywhere): parse_ply, visible set,
+ * keys, order, ndc, colour and opacity bit-exact, rot_scale within 4 x 2^-24 of
+ * its column norm, images within 1/255 but for quad-edge coverage flips.  This
+ * is a scalar restatement of the reference shaders; each function cites the
  * shader lines it follows.  Build with -O2 -ffp-contract=off -fno-fast-math so
  * that every product/sum below is one IEEE-754 binary32 rounding, evaluated in
  * GLSL order (column-major, left-to-right sums).

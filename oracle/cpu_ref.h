@@ -5,13 +5,13 @@
  * or calls this library; only tests/, the smoke check and the CPU-baseline arm
  * of bench.py do, and only as the checker / the timed CPU reference.
  *
- * Parity status: UNPINNED.  The reference (jaesung-cs/vkgs) ships no tests, no
- * fixtures and no CPU implementation, and its GLSL shaders cannot be executed
- * here (no Vulkan loader, no shader compiler, no software renderer).  This file
- * is a scalar restatement of the reference shaders with every floating-point
+ * Parity status: PINNED to the reference's shaders executed on the host
+ * (oracle/glsl/: the shader bodies compiled against a C++ GLSL subset; checked
+ * by tests/test_ref_pin.py and tests/golden/ref_fixtures.json).  This file is a
+ * scalar restatement of the reference shaders with every floating-point
  * operation order pinned (GLSL column-major, left-to-right sums, no FMA
- * contraction: build with -ffp-contract=off), which DEFINES the reference bits
- * for the visible set, the keys, the sorted order and the coverage decisions.
+ * contraction: build with -ffp-contract=off); its visible set, keys, sorted
+ * order, ndc, colour and opacity equal the shaders' bit for bit.
  *
  * Matrices are column-major float[16] exactly like glm::mat4: m[col*4 + row].
  */

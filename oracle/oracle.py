@@ -3,10 +3,11 @@
 TEST INFRASTRUCTURE ONLY.  Imported by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline arm of ``bench.py`` -- never by the product package.
 
-Parity status: unpinned.  The reference ships no tests, fixtures or CPU code,
-and its GLSL shaders cannot run here, so this scalar restatement of the shaders
-(every float operation in GLSL order, no FMA contraction) defines the reference
-bits; see ``cpu_ref.c`` for the per-function shader citations.
+Parity status: pinned.  The reference ships no tests, fixtures or CPU code and
+its GLSL shaders need a Vulkan stack, so ``oracle/glsl`` compiles the shader
+bodies for the host and ``tests/test_ref_pin.py`` holds this scalar restatement
+(every float operation in GLSL order, no FMA contraction) to their bits; see
+``cpu_ref.c`` for the per-function shader citations.
 """
 
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """Writes tests/golden/oracle_fixtures.json: regression fixtures of the oracle on small seeded scenes.
 
-These are NOT reference outputs (the reference ships no tests and its shaders cannot run here; parity
-with it is unpinned).  They pin the oracle's own results -- visible count, a digest of the sorted keys
+These are NOT reference outputs (those are tests/golden/ref_fixtures.json, written by
+make_ref_fixtures.py from the reference's shaders run on the host).  They pin the oracle's own results -- visible count, a digest of the sorted keys
 and ids, the fragment count and image checksums -- so that an unintended change to the restatement
 shows up as a failing CPU test.  Regenerate only when the restatement is changed on purpose:
 
