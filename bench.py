@@ -53,11 +53,16 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=9)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--splats", type=int, default=None, help="override the splat count (testing only)")
-    p.add_argument("--cpu-band-stride", type=int, default=8, help="CPU sample: blend every k-th 16-row band")
+    p.add_argument("--cpu-band-stride", type=int, default=8, help="one-core estimate: blend every 4k-th 16-row band")
+    p.add_argument("--cpu-seconds", type=float, default=120.0,
+                   help="reference arm: stop timing complete CPU frames after this long (at least 3 frames)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-forms", action="store_true", help="skip the batched / differentiation forms")
     p.add_argument("--only-form", choices=["batched", "differentiation", "batched_differentiation"], default=None,
                    help="run just this form and print its JSON (profiling; no headline line)")
+    p.add_argument("--form", choices=["plain", "batched", "batched_differentiation"], default="plain",
+                   help="plain: the headline frame (replicas under torchrun); batched / batched_differentiation: "
+                        "the view-sharded multi-GPU forms, one JSON line for the whole job")
     return p.parse_args()
 
 
@@ -150,8 +155,29 @@ def make_scene(n_override=None):
     return rows, syn.ply_offsets(), syn.workload_cameras(WORKLOAD), n
 
 
-def cpu_frames(oracle, act, cams, band_stride: int, steps: int, threads: int):
-    """Estimated seconds per frame on the host: full rank/sort/project + a band-sampled blend x stride."""
+def cpu_frames(oracle, act, cams, frames, first: int = 0):
+    """Seconds per COMPLETE frame on the host (timed, nothing extrapolated): cull/key/compaction, stable
+    sort, projection and the full blend of every pixel, for cameras first, first+1, ... (cycled)."""
+    from tests import scenes
+
+    out = []
+    for k in range(first, first + frames):
+        spec = cams[k % len(cams)]
+        c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=spec.width, height=spec.height,
+                          near=spec.near, far=spec.far)
+        cam = scenes.oracle_camera(oracle, c)
+        t0 = time.perf_counter()
+        key, idx = oracle.rank(act[0], cam)
+        key, idx = oracle.sort_kv(key, idx)
+        _, rec = oracle.project(*act, idx, cam)
+        oracle.raster(rec, spec.width, spec.height)
+        out.append(time.perf_counter() - t0)
+    return out
+
+
+def cpu_band_estimate(oracle, act, cams, band_stride: int, steps: int):
+    """Seconds per frame ESTIMATED from a sample: full cull/sort/projection + the blend of every
+    band_stride-th 16-row band (offset k % band_stride at step k), blend time x band_stride."""
     from tests import scenes
 
     out = []
@@ -382,33 +408,146 @@ def run_reference(args):
     act = oracle.parse_ply(rows, off)
     del rows
     threads = oracle.num_threads()
-    cpu_frames(oracle, act, cams, args.cpu_band_stride, max(args.warmup, 0), threads)
-    times = cpu_frames(oracle, act, cams, args.cpu_band_stride, args.steps, threads)
+    # Complete frames, each timed: one untimed frame pages the scene in, then K frames (camera k mod 9),
+    # capped so that the run stays within a few minutes; `steps` reports the frames actually timed.
+    cpu_frames(oracle, act, cams, 1 if args.warmup > 0 else 0)
+    t_start = time.perf_counter()
+    times = []
+    while len(times) < args.steps and (len(times) < 3 or time.perf_counter() - t_start < args.cpu_seconds):
+        times += cpu_frames(oracle, act, cams, 1, first=len(times))
     value = len(times) / sum(times)
-    # the same restatement on one core: one camera, a sparser band sample
+    # The same restatement on one core, estimated from a band sample (a complete one-core frame takes
+    # minutes): 4 steps, cameras 0-3, every 32nd 16-row band at offsets 0-3, blend time x32.
     oracle.set_num_threads(1)
     try:
-        one = cpu_frames(oracle, act, cams, 4 * args.cpu_band_stride, 1, 1)
+        stride = 4 * args.cpu_band_stride
+        one = cpu_band_estimate(oracle, act, cams, stride, 4)
     finally:
         oracle.set_num_threads(threads)
-    sample = (f"per step: full cull/key/sort/projection of all {n} splats + blend of every "
-              f"{args.cpu_band_stride}th 16-row band, blend time x{args.cpu_band_stride}")
+    sample = (f"{len(times)} complete frames (cameras 0..{len(times) - 1} mod 9) of all {n} splats: cull/key/"
+              "compaction, stable sort, projection and the full blend of every pixel, each timed")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "steps": len(times), "steps_requested": args.steps, "warmup": min(args.warmup, 1),
+        "ms_per_step": 1000 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD}: {n} splats, 1600x900, 9 cameras (8 on r=8 circle + r=20)",
-                   "l2": "inputs (816 MB) exceed L2"},
+        "config": {"workload": f"{WORKLOAD}: {n} splats (70% shell r=4, 30% uniform), 1600x900, 9 cameras "
+                               "(8 on an r=8 circle + 1 at r=20), SH degree 3 in binary16",
+                   "parallelism": f"host threads x{threads}", "l2": "inputs (816 MB) exceed L2; no flush"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
-                         "one_core": {"value": 1.0 / one[0], "unit": UNIT, "cores": 1,
-                                      "sample": f"camera 0: full cull/key/sort/projection + blend of 1 in "
-                                                f"{4 * args.cpu_band_stride} 16-row bands, blend time x"
-                                                f"{4 * args.cpu_band_stride}"}},
+                         "frame_s": [round(t, 3) for t in times],
+                         "one_core_estimate": {"value": 4.0 / sum(one), "unit": UNIT, "cores": 1, "steps": 4,
+                                               "sample": f"ESTIMATE: cameras 0-3, full cull/key/sort/projection "
+                                                         f"+ blend of every {stride}th 16-row band (offset k mod "
+                                                         f"{stride} at step k), blend time x{stride}"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's Vulkan shaders cannot run here (no graphics stack); this arm is the scalar "
-                "C restatement of those shaders (oracle/cpu_ref.c) on all host cores",
+                "C restatement of those shaders (oracle/cpu_ref.c, pinned to the shaders' own bits on the "
+                "host) on all host cores",
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_sharded_form(args):
+    """The view-sharded forms on N GPUs (one process per GPU under torchrun): every rank holds the whole
+    scene and takes its share of the views (vkgs_gb300.shard.view_shards: largest first, least-loaded
+    rank).  batched: a step renders the 64-view batch (1M splats) -- each rank its views in one captured
+    graph, no collective.  batched_differentiation: a step is one fwd+bwd of the 16-view batch (3M
+    splats) with the gradients all-reduced over NCCL (shard.train_step_sharded).  The batch is fixed as
+    N grows (strong scaling); value = whole-job views/s or it/s over the max-over-ranks time."""
+    import torch
+    import torch.distributed as dist
+
+    from vkgs_gb300 import Camera, Renderer, parse_ply, shard, synthetic as syn, train, train_params as tp
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    else:
+        import socket
+
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        dist.init_process_group("nccl", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    K, W = args.steps, max(args.warmup, 3)
+    if args.form == "batched":
+        rows, off, specs = syn.workload("batched")
+        splats = parse_ply(torch.from_numpy(rows).to(dev), off)
+        del rows
+        cams = [Camera.from_spec(sp) for sp in specs]
+        mine = shard.view_shards(cams, world)[rank]
+        colors = [torch.empty((c.height, c.width, 4), device=dev) for c in cams]
+        r = Renderer(splats.count, 1920, 1080)
+        r.set_batch_lanes(16)
+        for v in mine:
+            r.render_checked(splats, cams[v], color=colors[v])
+        shard.render_batched_sharded(r, splats, cams, colors, rank, world)
+        r.check()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            shard.render_batched_sharded(r, splats, cams, colors, rank, world)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            shard.render_batched_sharded(r, splats, cams, colors, rank, world)
+        step = g.replay
+        units, unit, metric = len(cams), "views/s", "batched views/s (1M splats, 64 views of 640x360..1920x1080)"
+        workload = f"batched: {splats.count} splats, 64 random cameras, sharded by view over {world} rank(s)"
+    else:
+        rows, _, specs = syn.workload("batched_grad")
+        raw = tp.from_rows(rows)
+        n = rows.shape[0]
+        del rows
+        cams = [Camera.from_spec(sp) for sp in specs]
+        params = {k: torch.tensor(v, device=dev, requires_grad=True) for k, v in raw.items()}
+        mine = shard.view_shards(cams, world)[rank]
+        r = Renderer(n, max(c.width for c in cams), max(c.height for c in cams))
+        r.set_batch_lanes(max(len(mine), 1))
+        with torch.no_grad():
+            pert = {k: torch.tensor(v, device=dev) for k, v in _perturbed(raw).items()}
+            targets = [t.clone() for t in train.render_batched(pert, cams, r)]
+            del pert
+
+        def step():
+            for t in params.values():
+                t.grad = None
+            shard.train_step_sharded(params, cams, lambda v, img: (img - targets[v]).abs().mean() / len(cams), r,
+                                     rank, world)
+
+        units, unit, metric = 1, "it/s", "batched fwd+bwd it/s (3M splats, 16 views per step)"
+        workload = f"batched_grad: {n} splats, 16 views per step, sharded by view over {world} rank(s), " \
+                   "gradients all-reduced (NCCL)"
+    for _ in range(W):
+        step()
+    r.check()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(K):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    dist.barrier()
+    r.check()
+    t = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    if rank == 0:
+        print(json.dumps({
+            "metric": metric, "value": units * K / (ms / 1e3), "unit": unit, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "parallelism": f"views sharded x{world}", "form": args.form,
+                       "views_on_rank0": len(mine)},
+            "gpu_launches": None}), flush=True)
+    dist.destroy_process_group()
     return 0
 
 
@@ -616,10 +755,11 @@ def run_ours(args):
             act = oracle.parse_ply(host_rows, off)
             del host_rows
             threads = oracle.num_threads()
-            times = cpu_frames(oracle, act, specs, args.cpu_band_stride, len(specs), threads)
+            times = cpu_frames(oracle, act, specs, 3)
             cpu = {"value": len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"each of the 9 cameras once: full cull/key/sort/projection + blend of every "
-                             f"{args.cpu_band_stride}th 16-row band, blend time x{args.cpu_band_stride}"}
+                   "sample": "3 complete frames (cameras 0, 1, 2), each timed: cull/key/compaction, stable sort, "
+                             "projection and the full blend of every pixel",
+                   "frame_s": [round(t, 3) for t in times]}
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {exc}"}
 
@@ -680,6 +820,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.form != "plain":
+        return run_sharded_form(args)
     return run_ours(args)
 
 

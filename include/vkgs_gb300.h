@@ -79,17 +79,19 @@ gs_status gs_sorter_sort_key_value_indirect(gs_sorter* sorter, gs_stream stream,
 gs_status gs_sorter_check(gs_sorter* sorter, gs_stream stream);
 
 /* No counterpart in the reference.  The same sort for callers that may not allocate device memory
- * (an engine callback that owns the whole memory budget, code running while other streams are in
- * flight -- cudaMalloc/cudaFree can synchronise the device -- or code recorded during stream
- * capture): no sorter handle, no storage argument, and no cudaMalloc/cudaFree on any path.  Its
+ * (an engine callback that owns the whole memory budget, or code running while other streams are in
+ * flight -- cudaMalloc/cudaFree can synchronise the device): no sorter handle, no storage argument,
+ * and no cudaMalloc/cudaFree on any path.  Its
  * scratch is one fixed device array inside this library (about 8.4 MB, held by every GPU that
  * loads the library until the process exits), so max_count may not exceed
  * GS_SORT_NOALLOC_MAX_COUNT (GS_ERROR_CAPACITY otherwise).  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the array: calls that may overlap on the GPU (other
+ * before any stream capture.  The address is kept per device ordinal, i.e. for the device's primary
+ * context (the runtime API's context): callers that make another driver-API context current on the
+ * same device are not supported.  All calls share the array: calls that may overlap on the GPU (other
  * streams, other threads) race and must be serialised by the caller.  device_error (optional device
  * word) receives the error bits: 1 = *count exceeded max_count and was clamped, 2 = a bounded device
- * wait gave up. */
+ * wait gave up; with device_error NULL those bits are discarded and nothing reports them. */
 #define GS_SORT_NOALLOC_MAX_COUNT (1u << 20)
 gs_status gs_sort_key_value_noalloc(gs_stream stream, uint32_t max_count, const uint32_t* count, uint32_t* keys,
                                     uint32_t* values, uint32_t* device_error);
@@ -214,8 +216,11 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
  * run on a lane: sub-contexts with their own scratch and stream, forked from `stream` and joined back
  * into it with events, so the batch is ordered on `stream` and can be captured in a CUDA graph as a
  * whole.  The shared pass keeps every view's records (72 bytes per splat and view, at most 64 views
- * at a time); they are allocated by the first batched call that needs them -- if that call is being
- * captured, it uses a per-lane cull instead.  With no lanes the views render one after another on
+ * at a time) in an arena allocated by the first batched call that needs it.  A later call that needs
+ * a larger arena (more views, or more splats after gs_context_reserve) replaces it, which synchronises
+ * the device and frees the old one -- but never while the call is being captured and never once any
+ * batched call has been captured with the arena (a captured graph keeps using its addresses): those
+ * calls use a per-lane cull instead, with the same results.  With no lanes the views render one after another on
  * `stream`.  gs_context_check afterwards reports every lane's errors and the summed statistics
  * (tile_pairs: the largest). */
 gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32_t n_views,
@@ -275,7 +280,9 @@ gs_status gs_train_forward(gs_context* context, const gs_train_params* params, c
  * each tile's list in reverse from the stored final transmittance (no per-pixel lists are stored) and
  * accumulates per-splat gradients warp-reduced, then atomically; the projection backward then runs per
  * splat through conic -> 2D covariance -> scale / quaternion, SH -> coefficients, and back to the means
- * (including the SH view direction).  Results are added into `grads`. */
+ * (including the SH view direction).  Results are added into `grads`.  Returns GS_ERROR_INVALID_ARGUMENT
+ * when the context has rendered anything since that forward, or was re-reserved (the forward's lists
+ * are gone). */
 gs_status gs_train_backward(gs_context* context, const gs_train_params* params, const gs_camera* camera,
                             const float* grad_rgba32f, const gs_train_grads* grads, gs_stream stream);
 
@@ -314,7 +321,9 @@ gs_status gs_viewer_check(gs_viewer* viewer, gs_stream stream);
  * GS_ERROR_CAPACITY otherwise), which keeps that view's forward state; the activation runs once.  The
  * backward runs every view's blend and projection backward concurrently and adds all views' gradients
  * into the one set of buffers (atomically), as a loss summed over the views requires.  Both calls are
- * ordered on `stream` (fork/join over the lanes' streams). */
+ * ordered on `stream` (fork/join over the lanes' streams).  The backward needs the same n_views as the
+ * last batched forward, with nothing rendered on the context or its lanes in between (a batched render
+ * would overwrite the views' records and lists): GS_ERROR_INVALID_ARGUMENT otherwise. */
 gs_status gs_train_forward_batched(gs_context* context, const gs_train_params* params, uint32_t n_views,
                                    const gs_camera* cameras, float* const* colors_rgba32f, gs_stream stream);
 gs_status gs_train_backward_batched(gs_context* context, const gs_train_params* params, uint32_t n_views,

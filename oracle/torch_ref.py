@@ -112,13 +112,16 @@ def rot_scale_inverse(cov2d):
         return m, drawn
 
 
-def render(means, log_scales, quats, opacity_logits, sh, cam, order, chunk=4096, mask_records=None):
+def render(means, log_scales, quats, opacity_logits, sh, cam, order, chunk=4096, mask_records=None, window=None):
     """RGBA (H, W, 4) float64 for splats `order` (sorted draw order, far to near), autograd-capable.
 
     mask_records: optional (V, 16) FP32 raster records of the same splats in the same order (the C
     oracle's): coverage is then decided in FP32 with the renderer's rounding (dx = px - cx,
-    u = m00 dx + m01 dy, one rounding per operation), so both sides blend the same (pixel, splat) set."""
+    u = m00 dx + m01 dy, one rounding per operation), so both sides blend the same (pixel, splat) set.
+    window: optional pixel rectangle (x0, x1, y0, y1), half-open: only those pixels are drawn and the
+    result is (y1 - y0, x1 - x0, 4) -- every pixel's value is the same as in the whole image."""
     W, H = int(cam["width"]), int(cam["height"])
+    x0, x1, y0, y1 = (0, W, 0, H) if window is None else (int(v) for v in window)
     idx = torch.as_tensor(order, dtype=torch.long)
     centre, cov2d, col, o, depth = project(means[idx], log_scales[idx], quats[idx], opacity_logits[idx], sh[idx], cam)
     m, drawn = rot_scale_inverse(cov2d)
@@ -133,13 +136,14 @@ def render(means, log_scales, quats, opacity_logits, sh, cam, order, chunk=4096,
     centre, conic, col, o, m, keep = (t.flip(0) for t in (centre, conic, col, o, m, keep))
     if rec is not None:
         rec = rec.flip(0)
-    ys, xs = torch.meshgrid(torch.arange(H, dtype=torch.float64), torch.arange(W, dtype=torch.float64), indexing="ij")
+    ys, xs = torch.meshgrid(torch.arange(y0, y1, dtype=torch.float64), torch.arange(x0, x1, dtype=torch.float64),
+                            indexing="ij")
     px = ((2 * xs + 1) / W - 1).reshape(-1)
     py = ((2 * ys + 1) / H - 1).reshape(-1)
     px32 = ((2 * xs.float() + 1) / torch.tensor(float(W), dtype=torch.float32) - 1).reshape(-1)
     py32 = ((2 * ys.float() + 1) / torch.tensor(float(H), dtype=torch.float32) - 1).reshape(-1)
     out = []
-    for s0 in range(0, W * H, chunk):
+    for s0 in range(0, px.shape[0], chunk):
         dx = px[None, s0:s0 + chunk] - centre[:, :1]
         dy = py[None, s0:s0 + chunk] - centre[:, 1:2]
         with torch.no_grad():
@@ -159,7 +163,7 @@ def render(means, log_scales, quats, opacity_logits, sh, cam, order, chunk=4096,
         rgb = (w[:, :, None] * col[:, None, :]).sum(0)
         alpha = (w * a).sum(0) + T[-1]
         out.append(torch.cat([rgb, alpha[:, None]], -1))
-    return torch.cat(out, 0).reshape(H, W, 4)
+    return torch.cat(out, 0).reshape(y1 - y0, x1 - x0, 4)
 
 
 def camera_dict(oracle_cam: dict) -> dict:

@@ -164,3 +164,86 @@ def test_batched_rejects_bad_targets(cuda):
             r.render_batched(splats, big[:1], [torch.empty((big[0].height, big[0].width, 4), device="cuda")])
     with pytest.raises(ValueError):
         r.render_batched(splats, cams, colors[:1])
+
+
+def test_batched_workload_at_size(cuda, oracle):
+    """The batched form at its own size: 1M splats (shell layout), the 64 random cameras of 640x360 ...
+    1920x1080, captured in one CUDA graph and replayed as the bench does with the autotuner's choice --
+    every view bit-identical to its single-view gs_render, and five views (the largest 1920x1080 ones
+    first) within 1/255 of the oracle's image."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer, parse_ply
+    from vkgs_gb300.autotune import autotune_batched
+
+    rows, off, specs = syn.workload("batched")
+    splats = parse_ply(torch.from_numpy(rows).cuda(), off)
+    cams = [Camera.from_spec(sp) for sp in specs]
+    colors = [torch.empty((c.height, c.width, 4), dtype=torch.float32, device="cuda") for c in cams]
+    r = Renderer(splats.count, 1920, 1080)
+    for c in cams:  # the bench sizes the pair capacity with single renders first
+        r.render_checked(splats, c)
+    choice = autotune_batched(r, splats, cams, colors, reps=1)
+    single = Renderer(splats.count, 1920, 1080)
+    single.set_slabs(choice.slabs)  # the same depth-slab schedule as the tuned batch
+    want = [single.render_checked(splats, c)[0].clone() for c in cams]
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        r.render_batched(splats, cams, colors)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        r.render_batched(splats, cams, colors)
+    for _ in range(2):
+        for c in colors:
+            c.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for k, (a, b) in enumerate(zip(colors, want)):
+            assert torch.equal(a, b), k
+    r.check()
+    act = scenes.activated(oracle, rows)
+    order = sorted(range(len(specs)), key=lambda k: -specs[k].width * specs[k].height)
+    picked = order[:2] + order[len(order) // 2: len(order) // 2 + 1] + order[-2:]
+    assert specs[picked[0]].width == 1920
+    for k in picked:
+        spec = specs[k]
+        c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=spec.width, height=spec.height)
+        o = oracle.render_frame(*act, scenes.oracle_camera(oracle, c), want_instances=False)
+        err = np.abs(colors[k].cpu().numpy().astype(np.float64) - o["image"]).max()
+        assert err <= 1.0 / 255.0, (k, err)
+
+
+def test_captured_batch_survives_a_larger_eager_batch(cuda):
+    """A batch captured with N views keeps replaying correctly after an eager batched call with 2N views
+    (the arena is not replaced while a captured graph may use it; the larger call culls per lane)."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer
+
+    _, splats, specs, cams, colors = _setup(60_000, 18, 4, 510)
+    more = [Camera.from_spec(sp) for sp in syn.random_cameras(8, seed=511)]
+    more_colors = [torch.empty((c.height, c.width, 4), device="cuda") for c in more]
+    single = Renderer(60_000, 1920, 1080)
+    want = [single.render_checked(splats, c)[0].clone() for c in cams]
+    want_more = [single.render_checked(splats, c)[0].clone() for c in more]
+    r = Renderer(60_000, 1920, 1080)
+    r.set_batch_lanes(4)
+    r.render_batched_checked(splats, cams, colors)  # the arena for 4 views exists before the capture
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        r.render_batched(splats, cams, colors)
+    r.render_batched_checked(splats, more, more_colors)  # needs 8 views' arena
+    for a, b in zip(more_colors, want_more):
+        assert torch.equal(a, b)
+    for _ in range(2):
+        for c in colors:
+            c.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip(colors, want):
+            assert torch.equal(a, b)
+    r.check()

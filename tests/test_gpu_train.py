@@ -198,3 +198,111 @@ def test_sharded_train_step_single_rank_matches_batched(cuda):
             assert rel <= 1e-5, (k, rel)
     finally:
         dist.destroy_process_group()
+
+
+def _footprint_window(rec, w, h):
+    """Pixel rectangle (x0, x1, y0, y1) holding every pixel centre a raster record's quad can cover."""
+    import math
+
+    cx, cy, hx, hy = float(rec[0]), float(rec[1]), float(rec[12]), float(rec[13])
+    x0 = max(0, math.floor((cx - hx + 1.0) * w / 2 - 0.5) - 1)
+    x1 = min(w, math.ceil((cx + hx + 1.0) * w / 2 - 0.5) + 2)
+    y0 = max(0, math.floor((cy - hy + 1.0) * h / 2 - 0.5) - 1)
+    y1 = min(h, math.ceil((cy + hy + 1.0) * h / 2 - 0.5) + 2)
+    return x0, x1, y0, y1
+
+
+def test_gradient_check_workload_at_size(cuda, oracle):
+    """The gradient-check workload at its stated size: 1,000 splats at 256x256.  CUDA gradients of every
+    parameter group within 1e-3 (relative norm) of torch-FP64 autograd, and, on 4 entries per group
+    (among the largest), FP64 central differences (h = 1e-6) of the loss agreeing with torch-FP64 autograd
+    to 1e-5 and with the CUDA gradient to 1e-3.  A central difference perturbs one splat, which changes
+    only the pixels its quad covers, so the loss is evaluated over that footprint's rectangle."""
+    import torch
+    from oracle import torch_ref
+    from vkgs_gb300 import Camera, Renderer, train
+
+    rows, off, specs = syn.workload("grad_check")
+    spec = specs[0]
+    assert rows.shape[0] == 1000 and (spec.width, spec.height) == (256, 256)
+    w, h = spec.width, spec.height
+    c = scenes.camera(oracle, spec.eye, fovy_deg=spec.fovy_deg, width=w, height=h)
+    act = scenes.activated(oracle, rows)
+    ocam = scenes.oracle_camera(oracle, c)
+    out = oracle.render_frame(*act, ocam)
+    _, rec = oracle.project(*act, out["index"], ocam)
+    assert out["count"] > 500
+    weights = np.random.default_rng(12).standard_normal((h, w, 4))
+
+    params = _gpu_params(rows)
+    img = train.render(params, scenes.product_camera(c), Renderer(1000, w, h))
+    (img * torch.tensor(weights, dtype=torch.float32, device="cuda")).sum().backward()
+
+    p64 = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True) for k, v in tp.from_rows(rows).items()}
+    cam = torch_ref.camera_dict(c)
+    args = lambda: (p64["means"], p64["log_scales"], p64["quats"], p64["opacity_logits"], p64["sh"], cam, out["index"])
+    img64 = torch_ref.render(*args(), mask_records=rec)
+    (img64 * torch.tensor(weights)).sum().backward()
+    assert np.abs(img.detach().cpu().numpy() - img64.detach().numpy()).max() <= 1.0 / 255.0
+    grads = {}
+    for name in train.NAMES:
+        g = params[name].grad.double().cpu()
+        g64 = p64[name].grad.clone()
+        grads[name] = (g, g64)
+        rel = float((g - g64).norm() / g64.norm())
+        assert rel <= GRAD_RTOL, (name, rel)
+
+    record_of = {int(s): r for r, s in enumerate(out["index"])}
+    rng = np.random.default_rng(5)
+    for name in train.NAMES:
+        g, g64 = grads[name]
+        flat = g64.reshape(g64.shape[0], -1).abs()
+        top = torch.argsort(flat.reshape(-1), descending=True)[:40].numpy()
+        for pick in rng.choice(top, 4, replace=False):
+            i, j = divmod(int(pick), flat.shape[1])
+            idx = (i,) if g64.dim() == 1 else (i, j)
+            win = _footprint_window(rec[record_of[i]], w, h)
+            wt = torch.tensor(weights[win[2]:win[3], win[0]:win[1]])
+
+            def loss():
+                return (torch_ref.render(*args(), mask_records=rec, window=win) * wt).sum()
+
+            fd = torch_ref.central_difference(loss, p64[name].data, idx)
+            scale = max(abs(fd), 0.1 * float(flat.max()))
+            assert abs(float(g64[idx]) - fd) <= 1e-5 * max(1.0, abs(fd)), (name, idx, float(g64[idx]), fd)
+            assert abs(float(g[idx]) - fd) <= 1e-3 * scale, (name, idx, float(g[idx]), fd)
+
+
+def test_backward_refuses_overwritten_forward_state(cuda, oracle):
+    """A render between a differentiable forward and its backward overwrites the forward's tile lists:
+    the backward is refused (GS_ERROR_INVALID_ARGUMENT) instead of reading another frame's lists, for
+    the one-view and the batched form; with nothing in between it runs."""
+    import torch
+    from vkgs_gb300 import Camera, GsError, Renderer, parse_ply, train
+
+    n = 5_000
+    rows = syn.splat_rows(n, 17)
+    cams = [Camera.from_spec(sp) for sp in syn.random_cameras(3, seed=509, resolutions=[(160, 120), (128, 96)])]
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    r = Renderer(n, 160, 120)
+    img = train.render(_gpu_params(rows), cams[0], r)
+    r.render(splats, cams[1])
+    with pytest.raises(GsError) as e:
+        img.sum().backward()
+    assert e.value.status == 1
+    img = train.render(_gpu_params(rows), cams[0], r)
+    img.sum().backward()  # nothing in between: fine
+
+    rb = Renderer(n, 160, 120)
+    rb.set_batch_lanes(len(cams))
+    colors = [torch.empty((c.height, c.width, 4), device="cuda") for c in cams]
+    for between in (lambda: rb.render_batched(splats, cams, colors),
+                    lambda: train.forward_batched(rb, [t.detach() for t in _gpu_params(rows).values()], cams[:2])):
+        imgs = train.render_batched(_gpu_params(rows), cams, rb)
+        between()
+        with pytest.raises(GsError) as e:
+            sum(i.sum() for i in imgs).backward()
+        assert e.value.status == 1
+    imgs = train.render_batched(_gpu_params(rows), cams, rb)
+    sum(i.sum() for i in imgs).backward()
+    rb.check()

@@ -89,3 +89,48 @@ def test_viewer_frames_in_flight_rejects_bad_counts(cuda):
     for n in (0, 9):
         with pytest.raises((GsError, ValueError)):
             Viewer(r, splats, cam, [torch.zeros((180, 320, 4), device="cuda")] * max(n, 1), frames_in_flight=n)
+
+
+def test_bench_viewer_four_frames_in_flight_equal_direct_renders(cuda):
+    """The headline configuration as the bench runs it: 6M splats (shell layout), 1600x900, the nine
+    cameras cycled for two laps through gs_viewer_submit with four frames in flight, the pair capacity
+    reserved from counted frames -- every frame bit-identical to a direct gs_render of its camera."""
+    import torch
+    from vkgs_gb300 import Camera, Renderer, Viewer, parse_ply
+
+    rows = syn.splat_rows(6_000_000, 1, "shell")
+    splats = parse_ply(torch.from_numpy(rows).cuda(), syn.ply_offsets())
+    del rows
+    cams = [Camera.from_spec(s) for s in syn.circle_cameras()]
+    direct = Renderer(6_000_000, 1600, 900)
+    want = [direct.render_checked(splats, c)[0].clone() for c in cams]
+    direct.close()
+    r = Renderer(6_000_000, 1600, 900)
+    r.count_fragments(True)
+    pairs = max(r.render_checked(splats, c)[1]["tile_pairs"] for c in cams)
+    r.count_fragments(False)
+    r.reserve(max_tile_pairs=int(pairs * 1.05) + 1024)
+    v = Viewer(r, splats, cams[0], torch.zeros((900, 1600, 4), device="cuda"), frames_in_flight=4)
+    # as the bench's end-to-end loop: a slot's image is copied on a side stream after its frame, and the
+    # slot is drawn into again only after that copy, so up to four frames overlap on the GPU
+    main = torch.cuda.current_stream()
+    copier = torch.cuda.Stream()
+    copied = [torch.cuda.Event() for _ in range(4)]
+    started, got = set(), []
+    for k in range(2 * len(cams)):
+        slot = v.next_slot
+        if slot in started:
+            main.wait_event(copied[slot])
+        started.add(slot)
+        assert v.submit(cams[k % len(cams)], stream=main) == slot
+        v.wait(slot, copier)
+        with torch.cuda.stream(copier):
+            got.append(v.colors[slot].clone())
+        copied[slot].record(copier)
+    main.wait_stream(copier)
+    v.check(main)
+    torch.cuda.synchronize()
+    for k, img in enumerate(got):
+        assert torch.equal(img, want[k % len(cams)]), k
+    v.close()
+    r.check()

@@ -92,3 +92,71 @@ def test_render_batched_sharded_renders_exactly_the_ranks_views():
         assert r.got == ([cams[v] for v in mine], [colors[v] for v in mine])
         seen += mine
     assert sorted(seen) == list(range(10))
+
+
+def _fake_render_batched(params, cameras, renderer):
+    """A CPU autograd stand-in for train.render_batched: one image per camera, every parameter group
+    entering it (the sharded step's host logic is what is under test, not the kernels)."""
+    out = []
+    for c in cameras:
+        s = c.width / 10.0 + c.height / 7.0
+        base = ((params["means"] * s).sum() + (params["log_scales"] ** 2).sum() * 0.1 + params["quats"].sin().sum()
+                + torch.sigmoid(params["opacity_logits"]).sum() + (params["sh"] * s).cos().sum())
+        ramp = torch.linspace(0.0, 1.0, c.height * c.width * 4).reshape(c.height, c.width, 4)
+        out.append(base * ramp + ramp * s)
+    return tuple(out)
+
+
+def _train_inputs():
+    g = torch.Generator().manual_seed(3)
+    n = 7
+    params = {"means": torch.randn((n, 3), generator=g), "log_scales": torch.randn((n, 3), generator=g),
+              "quats": torch.randn((n, 4), generator=g), "opacity_logits": torch.randn((n,), generator=g),
+              "sh": torch.randn((n, 48), generator=g)}
+    cams = [_Cam(w, h) for w, h in [(8, 6), (12, 4), (5, 5), (9, 7), (6, 10)]]
+    targets = [torch.rand((c.height, c.width, 4), generator=g) * 40.0 for c in cams]
+    return params, cams, targets
+
+
+def _train_worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    from vkgs_gb300 import train
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        train.render_batched = _fake_render_batched
+        params, cams, targets = _train_inputs()
+        params = {k: v.clone().requires_grad_(True) for k, v in params.items()}
+        loss = shard.train_step_sharded(params, cams, lambda v, img: (img - targets[v]).abs().mean(), None, rank,
+                                        world)
+        out[rank] = {"loss": float(loss), "grads": {k: params[k].grad.tolist() for k in train.NAMES},
+                     "views": shard.view_shards(cams, world)[rank]}
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_train_step_two_ranks_equals_the_sum_over_all_views():
+    """shard.train_step_sharded over two gloo ranks: each rank renders only its views, and after the
+    one all-reduce every rank holds the gradient of the loss summed over ALL views, and the summed
+    loss -- equal to a single process that renders every view."""
+    from vkgs_gb300 import train
+
+    world = 2
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_train_worker, args=(world, _free_port(), out), nprocs=world, start_method="spawn", join=True)
+    params, cams, targets = _train_inputs()
+    params = {k: v.clone().requires_grad_(True) for k, v in params.items()}
+    imgs = _fake_render_batched(params, cams, None)
+    loss = sum((img - t).abs().mean() for img, t in zip(imgs, targets))
+    loss.backward()
+    assert sorted(out[0]["views"] + out[1]["views"]) == list(range(len(cams)))
+    assert out[0]["views"] and out[1]["views"]
+    for rank in range(world):
+        assert out[rank]["loss"] == pytest.approx(float(loss), rel=1e-6)
+        for k in train.NAMES:
+            got = torch.tensor(out[rank]["grads"][k])
+            assert torch.allclose(got, params[k].grad, rtol=1e-5, atol=1e-6), k

@@ -65,3 +65,15 @@ def test_autograd_matches_central_differences(oracle):
             assert abs(g - fd) <= 1e-5 * max(1.0, abs(fd)), (name, idx, g, fd)
             checked += 1
     assert checked == 20
+
+
+def test_window_render_equals_the_crop(oracle):
+    from oracle import torch_ref
+
+    rows, c, out = _scene(oracle, 300, 33, (0.5, 0.0, 5.0), 80, 60)
+    p = _params(rows)
+    cam = torch_ref.camera_dict(c)
+    full = torch_ref.render(p["means"], p["log_scales"], p["quats"], p["opacity_logits"], p["sh"], cam, out["index"])
+    win = torch_ref.render(p["means"], p["log_scales"], p["quats"], p["opacity_logits"], p["sh"], cam, out["index"],
+                           window=(13, 47, 5, 52))
+    assert torch.equal(win, full[5:52, 13:47])

@@ -1,9 +1,9 @@
 """The allocation-free key/value sort, checked against the allocating sorter.
 
 Some callers of this library may not call cudaMalloc: an engine callback that owns the whole
-device-memory budget, code running while other streams are in flight (allocation can synchronise the
-device), or code recorded during stream capture.  gs_sort_key_value_noalloc serves them with its
-scratch in a fixed device array inside the library.  This file calls it through the C ABI and
+device-memory budget, or code running while other streams are in flight (allocation can synchronise
+the device).  gs_sort_key_value_noalloc serves them with its scratch in a fixed device array inside
+the library.  This file calls it through the C ABI and
 compares its result with gs_sorter_sort_key_value_indirect on the same inputs, on consecutive calls
 (the shared array keeps each call's leftovers), plus the rejection of a size beyond its maximum.
 It is collected last so that a failure here never hides the result of another test.
@@ -68,3 +68,50 @@ def test_noalloc_sort_rejects_sizes_beyond_its_maximum(cuda):
     st = lib.gs_sort_key_value_noalloc(None, L.GS_SORT_NOALLOC_MAX_COUNT + 1, _ptr(cnt), _ptr(k), _ptr(k), None)
     assert st == L.GS_ERROR_CAPACITY
     assert lib.gs_sort_key_value_noalloc(None, 8, None, _ptr(k), _ptr(k), None) == L.GS_ERROR_INVALID_ARGUMENT
+
+
+def test_noalloc_sort_takes_no_device_memory(cuda):
+    """What the entry point exists for: after the first call on the device (which looks up the fixed
+    array's address), its calls take no device memory -- free device memory is the same before and
+    after three calls on fresh keys -- and each result equals the allocating sorter's."""
+    import torch
+    from vkgs_gb300 import Sorter
+    from vkgs_gb300 import _lib as L
+
+    lib = L.load()
+    n = 200_000
+    rng = np.random.default_rng(77)
+    k_buf = torch.empty(n, dtype=torch.int32, device="cuda")
+    v_buf = torch.empty(n, dtype=torch.int32, device="cuda")
+    cnt = torch.tensor([n], dtype=torch.int32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sorter = Sorter()
+    stream = torch.cuda.current_stream()
+
+    def call():
+        return lib.gs_sort_key_value_noalloc(ctypes.c_void_p(stream.cuda_stream), n, _ptr(cnt), _ptr(k_buf),
+                                             _ptr(v_buf), _ptr(err))
+
+    def load(keys, vals):
+        k_buf.copy_(torch.from_numpy(keys.view(np.int32)))
+        v_buf.copy_(torch.from_numpy(vals.view(np.int32)))
+
+    inputs = [_inputs(rng, n) for _ in range(3)]
+    wants = []
+    for keys, vals in inputs:
+        k_ref = torch.from_numpy(keys.view(np.int32)).cuda()
+        v_ref = torch.from_numpy(vals.view(np.int32)).cuda()
+        sorter.sort_key_value(k_ref, v_ref, count=n)
+        sorter.check()
+        wants.append((k_ref, v_ref))
+    load(*inputs[0])
+    assert call() == L.GS_SUCCESS  # the first call on this device does the set-up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for kv, (k_ref, v_ref) in zip(inputs, wants):
+        load(*kv)
+        assert call() == L.GS_SUCCESS
+        torch.cuda.synchronize()
+        assert torch.equal(k_buf, k_ref) and torch.equal(v_buf, v_ref)
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert int(err.item()) == 0

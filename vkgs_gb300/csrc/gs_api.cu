@@ -99,6 +99,10 @@ struct gs_context {
   u32* train_nproc = nullptr;      // per slab and pixel: list entries blended
   u32 train_slabs = 1;             // depth slabs of the last differentiable forward
   const float4* train_record = nullptr;  // the records that forward drew (its backward reads them)
+  // Frames recorded on this context, and which of them was the last differentiable forward: a
+  // backward whose forward state (tile lists, blended counts, records) was overwritten since by another
+  // frame on this context is refused instead of reading another frame's lists.
+  u64 frame_gen = 0, train_gen = 0;
   // The differentiable forward uses the slab schedule from this many splats on; below it the per-slab
   // fixed cost (seven more launches, the blended-count clears) outweighs the pairs it saves (measured:
   // 200k splats at 800x800, one slab 0.86 ms per fwd+bwd step vs 0.94 ms with two; 3M splats x 16
@@ -112,6 +116,10 @@ struct gs_context {
   char* batch_arena = nullptr;  // per-view cull outputs of the batched form (see batch_buffers)
   size_t batch_bytes = 0;
   u32 batch_views = 0, batch_n = 0;
+  u64 batch_gen = 0;        // writes into the batch arena (shared culls) and its reallocations
+  u64 train_batch_gen = 0;  // batch_gen right after the last batched differentiable forward (0: no arena)
+  u32 train_views = 0;      // views of the last batched differentiable forward
+  bool batch_captured = false;  // a batched call was recorded into a stream capture with the arena
   gs_context* lane[GS_MAX_LANES] = {};
   cudaStream_t lane_stream[GS_MAX_LANES] = {};
   cudaEvent_t lane_join[GS_MAX_LANES] = {};
@@ -437,6 +445,7 @@ static void free_batch_buffers(gs_context* c) {
   if (c->batch_arena) {
     cudaDeviceSynchronize();
     cudaFree(c->batch_arena);
+    ++c->batch_gen;
   }
   c->batch_arena = nullptr;
   c->batch_bytes = 0;
@@ -521,6 +530,7 @@ gs_status gs_context_reserve(gs_context* c, const gs_context_options* o) {
   }
   if (n == c->max_splats && w == c->max_width && h == c->max_height && pairs == c->pair_capacity) return GS_SUCCESS;
   if (cudaDeviceSynchronize() != cudaSuccess) return GS_ERROR_CUDA;
+  c->train_gen = 0;  // the differentiable forward's state lived in the old arena
   return context_allocate(c, n, w, h, pairs);
 }
 
@@ -577,6 +587,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   gs_frame_outputs none{};
   const gs_frame_outputs& o = outs ? *outs : none;
   c->last_batched = false;
+  c->train_gen = train ? ++c->frame_gen : (++c->frame_gen, 0);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const u32 n = s->count;
   const u32 W = cam->width, H = cam->height;
@@ -838,6 +849,7 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
   gs_status v = check_train_params(c, p, cam);
   if (v == GS_SUCCESS) v = check_train_grads(p, g);
   if (v != GS_SUCCESS) return v;
+  if (c->train_gen == 0 || c->train_gen != c->frame_gen) return GS_ERROR_INVALID_ARGUMENT;  // state overwritten
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if ((v = blend_backward(c, p, cam, grad_rgba, st)) != GS_SUCCESS) return v;
   return project_backward(&c, cam, 1, p, g, st);
@@ -885,9 +897,16 @@ static BatchLayout batch_layout(u32 views, u32 n) {
 }
 
 static bool batch_buffers(gs_context* c, u32 views, cudaStream_t st) {
-  if (c->batch_arena && views <= c->batch_views && c->max_splats <= c->batch_n) return true;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return false;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return false;
+  const bool capturing = cap != cudaStreamCaptureStatusNone;
+  if (c->batch_arena && views <= c->batch_views && c->max_splats <= c->batch_n) {
+    c->batch_captured |= capturing;
+    return true;
+  }
+  // Growing frees the arena.  Never while capturing, and never once a capture has recorded the arena's
+  // addresses: a graph holding them would replay into freed memory.  Those calls cull per lane instead.
+  if (capturing || c->batch_captured) return false;
   free_batch_buffers(c);
   const BatchLayout b = batch_layout(views, c->max_splats);
   if (cudaMalloc(&c->batch_arena, b.total) != cudaSuccess) {
@@ -915,6 +934,7 @@ static gs_status shared_cull(gs_context* c, const gs_splats* s, const float* sh3
                              cudaStream_t st) {
   const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
   char* base = c->batch_arena;
+  ++c->batch_gen;
   u32* tickets = reinterpret_cast<u32*>(base) + kMaxBatchViews;
   u64* status = reinterpret_cast<u64*>(base + b.status_off);
   if (cudaMemsetAsync(base, 0, b.head_bytes, st) != cudaSuccess) return GS_ERROR_CUDA;
@@ -1011,6 +1031,8 @@ gs_status gs_train_forward_batched(gs_context* c, const gs_train_params* p, uint
     if (r != GS_SUCCESS) return r;
   }
   c->last_batched = true;
+  c->train_batch_gen = shared ? c->batch_gen : 0;
+  c->train_views = n_views;
   return join_lanes(c, n_views, st);
 }
 
@@ -1025,6 +1047,12 @@ gs_status gs_train_backward_batched(gs_context* c, const gs_train_params* p, uin
   }
   gs_status r = check_train_grads(p, g);
   if (r != GS_SUCCESS || n_views == 0) return r;
+  // the forward state of every view must still be the last batched differentiable forward's: its
+  // lanes' lists and, with the shared cull, its records in the batch arena
+  if (n_views != c->train_views) return GS_ERROR_INVALID_ARGUMENT;
+  if (c->train_batch_gen != 0 && c->train_batch_gen != c->batch_gen) return GS_ERROR_INVALID_ARGUMENT;
+  for (u32 v = 0; v < n_views; ++v)
+    if (c->lane[v]->train_gen == 0 || c->lane[v]->train_gen != c->lane[v]->frame_gen) return GS_ERROR_INVALID_ARGUMENT;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if ((r = fork_lanes(c, n_views, st)) != GS_SUCCESS) return r;
   for (u32 v = 0; v < n_views; ++v) {  // the views' blend backwards run concurrently

@@ -1,9 +1,8 @@
 // gs_noalloc.cu -- the key/value sort for callers that cannot allocate device memory.
 //
 // Some callers may not call cudaMalloc/cudaFree at all: a per-frame callback of a host engine that
-// owns the whole device-memory budget, code that runs while other streams are in flight (allocation
-// and release can synchronise the device), or code recorded during stream capture.  This entry point
-// takes only the caller's keys, values and count and runs the same radix sort as
+// owns the whole device-memory budget, or code that runs while other streams are in flight
+// (allocation and release can synchronise the device).  This entry point takes only the caller's keys, values and count and runs the same radix sort as
 // gs_sorter_sort_key_value_indirect, with all of its scratch in the fixed array below.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads this library holds it
