@@ -617,6 +617,22 @@ def run_ours(args):
     stage = r.stage_times(K)
     r.enable_timing(False)
 
+    # The same frames with the cull's partitions staged in shared memory by bulk copies (faster alone,
+    # slower with frames in flight; reported beside the default)
+    r.set_cull_staging(True)
+    r.enable_timing(True)
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(K):
+        r.render(splats, cams[k % len(cams)], color=color)
+    e1.record()
+    torch.cuda.synchronize()
+    r.check()
+    staged_ms = e0.elapsed_time(e1) / K
+    staged_stage = r.stage_times(K)
+    r.enable_timing(False)
+    r.set_cull_staging(False)
+
     # (splat, tile) pairs binned per camera on the timed path (depth slabs, finished tiles skipped)
     emitted = []
     for cam in cams:
@@ -801,6 +817,12 @@ def run_ours(args):
                                 "form": "gs_viewer_frame: each frame waits for the previous one"},
         "direct_render": {"frames_per_s": world / (direct_ms / 1e3), "ms_per_frame": direct_ms,
                           "form": "one gs_render call per step (stages_ms are measured on this path)"},
+        "direct_render_staged_cull": {
+            "frames_per_s": world / (staged_ms / 1e3), "ms_per_frame": staged_ms,
+            "cull_project_ms": float(staged_stage[:, 0].mean()),
+            "cull_project_gbs": float(cull_bytes.sum() / (staged_stage[:, 0].sum() / 1e3) / 1e9),
+            "form": "gs_render with gs_context_set_cull_staging(1): cull partitions staged in shared memory "
+                    "by bulk copies"},
     }
     if not args.no_forms:
         line["batched"] = batched_form(dev, quick=args.steps < 9)

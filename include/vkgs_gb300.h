@@ -226,6 +226,16 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
 gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32_t n_views,
                             const gs_camera* cameras, const gs_target* targets, gs_stream stream);
 
+/* No counterpart in the reference.  1 = the plain path's cull + projection streams each 256-splat
+ * partition of the splat buffers into shared memory with bulk copies (two partitions in flight per
+ * CTA, a control warp resolving the compaction offsets off the compute warps' path); 0 (default) =
+ * per-thread loads.  Results are identical.  Staged, the pass alone is faster (0.237 vs 0.254 ms on
+ * 6M splats, 66 vs 62 % of HBM bandwidth) and so is a single frame, but its 70 KB of shared memory
+ * per CTA keeps other frames' kernels off the SMs while it runs, which costs throughput with frames
+ * in flight (4 slots: 763 vs 782 frames/s).  Needs 16-byte aligned position, cov3d, opacity and SH
+ * buffers (otherwise the per-thread form runs); not used by the differentiable path (FP32 SH). */
+gs_status gs_context_set_cull_staging(gs_context* context, int enable);
+
 /* Batched form: 1 (default) = the shared cull + projection pass above, 0 = each lane culls its views. */
 gs_status gs_context_set_batch_shared_cull(gs_context* context, int enable);
 

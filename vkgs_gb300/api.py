@@ -255,6 +255,11 @@ class Renderer:
         _check(self._lib.gs_context_set_batch_lanes(self._h, int(lanes)), "gs_context_set_batch_lanes")
         self._lanes = int(lanes)
 
+    def set_cull_staging(self, enable: bool = True) -> None:
+        """Plain path: stream the cull's splat partitions into shared memory with bulk copies (faster
+        alone, slower with frames in flight; same results)."""
+        _check(self._lib.gs_context_set_cull_staging(self._h, int(bool(enable))), "gs_context_set_cull_staging")
+
     def set_batch_shared_cull(self, enable: bool = True) -> None:
         """Batched form: one cull + projection pass for all views (default) or one per lane."""
         _check(self._lib.gs_context_set_batch_shared_cull(self._h, int(bool(enable))), "set_batch_shared_cull")

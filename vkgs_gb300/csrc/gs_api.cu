@@ -68,6 +68,7 @@ struct gs_context {
   u32 max_splats = 0, max_width = 0, max_height = 0, max_tiles = 0, pair_capacity = 0;
   int count_fragments = 0;
   float t_floor = 1e-4f;  // early stop: remaining contributions move no channel by more than this
+  bool staged_cull = false;  // plain path: stage each cull partition in shared memory with bulk copies
   u32 epoch = 1;
   char* arena = nullptr;
   size_t arena_bytes = 0;
@@ -180,7 +181,7 @@ static void context_layout(Carver& cv, gs_context* t, u32 max_splats, u32 max_wi
     t->pair_key = cv.take<u32>(pairs);
     t->pair_splat = cv.take<u32>(pairs);
     t->status_bytes_begin = cv.offset;
-    t->cull_status = cv.take<u64>((n + kCullTile - 1) / kCullTile);
+    t->cull_status = cv.take<u64>((n + kCullStatusSplats - 1) / kCullStatusSplats);
     t->radix_status_words = radix_status_words(n);
     t->radix_status = cv.take<u64>(t->radix_status_words);
     t->status_bytes_end = cv.offset;
@@ -413,7 +414,8 @@ gs_status gs_context_create(gs_context** out, const gs_context_options* o) {
   gs_context* c = new (std::nothrow) gs_context();
   if (!c) return GS_ERROR_OUT_OF_MEMORY;
   if (cudaGetDevice(&c->device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
+      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      cull_stream_init() != cudaSuccess) {
     delete c;
     return GS_ERROR_CUDA;
   }
@@ -552,6 +554,12 @@ gs_status gs_context_set_train_slab_min(gs_context* c, uint32_t splats) {
   return GS_SUCCESS;
 }
 
+gs_status gs_context_set_cull_staging(gs_context* c, int enable) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  c->staged_cull = enable != 0;
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_set_transmittance_floor(gs_context* c, float t_floor) {
   if (!c || !(t_floor > 0.0f) || !(t_floor <= 1.0f / 255.0f)) return GS_ERROR_INVALID_ARGUMENT;
   c->t_floor = t_floor;
@@ -634,6 +642,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   ca.epoch = 1;
   ca.err = c->err;
   ca.num_sms = c->num_sms;
+  ca.staged = c->staged_cull ? 1 : 0;
   if (!pre) GS_TRY(launch_cull_project(fc, ca, st));
   GS_MARK(1);
 
@@ -1119,7 +1128,7 @@ static gs_status capture_slot(ViewerSlot& sl, const gs_splats* s, const gs_camer
     if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
     cudaKernelNodeParams kp{};
     if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) continue;
-    if (kp.func != cull_project_kernel()) continue;
+    if (!is_cull_kernel(kp.func)) continue;
     sl.cull = node;
     sl.cull_params = kp;
     sl.cull_args = *reinterpret_cast<const CullArgs*>(kp.kernelParams[1]);
@@ -1157,6 +1166,7 @@ gs_status gs_viewer_create_frames(gs_viewer** out, gs_context* c, const gs_splat
       gs_context_set_slabs(sl.ctx, c->slab_count, c->slab_end);
       gs_context_set_count_fragments(sl.ctx, c->count_fragments);
       gs_context_set_transmittance_floor(sl.ctx, c->t_floor);
+      gs_context_set_cull_staging(sl.ctx, c->staged_cull);
     }
     const gs_status st = capture_slot(sl, s, cam, &targets[i]);
     if (st != GS_SUCCESS) return fail(st);

@@ -93,6 +93,41 @@ __device__ __forceinline__ u32 lb_resolve(u64* status, u32 stride, u32 p, u32 ep
   return exclusive;
 }
 
+// lb_resolve by a whole warp: lane l examines predecessor p-1-l (then 32 further back per step), so a
+// walk over predecessors that have published only their aggregates costs one round trip per 32 of them.
+// Every lane returns the exclusive prefix; lane 0 publishes the inclusive one.  Waits are bounded.
+__device__ __forceinline__ u32 lb_resolve_warp(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
+  const u32 lane = threadIdx.x & 31u;
+  u32 exclusive = 0;
+  for (int top = (int)p - 1; top >= 0; top -= 32) {
+    const int j = top - (int)lane;
+    u32 flag = LB_INCLUSIVE, value = 0;  // lanes beyond partition 0 stand for an empty inclusive prefix
+    if (j >= 0) {
+      u64 s = ld_relaxed_u64(status + (size_t)j * stride);
+      for (u32 spins = 0; (u32)(s >> 32) != epoch || ((u32)(s >> 30) & 3u) == 0;) {
+        if (++spins > kMaxSpins) {
+          atomicOr(err, ERR_TIMEOUT);
+          s = lb_pack(epoch, LB_INCLUSIVE, 0);
+          break;
+        }
+        __nanosleep(32);
+        s = ld_relaxed_u64(status + (size_t)j * stride);
+      }
+      flag = (u32)(s >> 30) & 3u;
+      value = (u32)s & 0x3fffffffu;
+    }
+    const u32 incl = __ballot_sync(0xffffffffu, flag == LB_INCLUSIVE);
+    const u32 stop = incl ? (u32)(__ffs(incl) - 1) : 31u;  // the nearest inclusive prefix ends the walk
+    u32 v = lane <= stop ? value : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    exclusive += v;
+    if (incl) break;
+  }
+  if (lane == 0 && p > 0) st_relaxed_u64(status + (size_t)p * stride, lb_pack(epoch, LB_INCLUSIVE, exclusive + aggregate));
+  return exclusive;
+}
+
 __device__ __forceinline__ u32 lookback(u64* status, u32 stride, u32 p, u32 epoch, u32 aggregate, u32* err) {
   lb_publish(status, stride, p, epoch, aggregate);
   return lb_resolve(status, stride, p, epoch, aggregate, err);

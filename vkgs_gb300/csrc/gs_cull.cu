@@ -56,18 +56,32 @@ __device__ __forceinline__ void unpack_half8(const uint4 q, float f[8]) {
   }
 }
 
-// SH32: FP32 coefficients (the differentiable path) instead of binary16 -- a separate instantiation, so
-// the plain path's kernel keeps its register count.
+// The projection of one visible splat from its values: c0..c5 = cov3d, shv = its 48 binary16 SH as
+// 6 x 16 bytes (global memory, or shared memory with SMEM), o = opacity.  SH32: FP32 coefficients read
+// from a.sh32 instead (the differentiable path) -- a separate instantiation, so the plain path keeps
+// its register count.
+template <bool SH32, bool SMEM = false>
+__device__ __forceinline__ void project_values(const FrameConst& fc, const CullArgs& a, u32 id, float x0, float y0,
+                                               float z0, float c0, float c1, float c2, float c3, float c4, float c5,
+                                               const uint4* shv, float o);
+
 template <bool SH32>
 __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, float x0, float y0, float z0) {
+  const float* cv = a.cov3d + 6 * (size_t)id;
+  project_values<SH32>(fc, a, id, x0, y0, z0, __ldg(cv + 0), __ldg(cv + 1), __ldg(cv + 2), __ldg(cv + 3),
+                       __ldg(cv + 4), __ldg(cv + 5), reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)id),
+                       __ldg(a.opacity + id));
+}
+
+template <bool SH32, bool SMEM>
+__device__ __forceinline__ void project_values(const FrameConst& fc, const CullArgs& a, u32 id, float x0, float y0,
+                                               float z0, float c0, float c1, float c2, float c3, float c4, float c5,
+                                               const uint4* shv, float o) {
   // direction for SH in model space (projection.comp:85-87); normalize = v / sqrt(dot(v, v))
   const float ddx = x0 - fc.cam_m[0], ddy = y0 - fc.cam_m[1], ddz = z0 - fc.cam_m[2];
   const float dl = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
   const float x = ddx / dl, y = ddy / dl, z = ddz / dl;
 
-  const float* cv = a.cov3d + 6 * (size_t)id;
-  const float c0 = __ldg(cv + 0), c1 = __ldg(cv + 1), c2 = __ldg(cv + 2), c3 = __ldg(cv + 3), c4 = __ldg(cv + 4),
-              c5 = __ldg(cv + 5);
   float C[9] = {c0, c1, c2, c1, c3, c4, c2, c4, c5};  // mat3(v0, v0.y, v1.xy, v0.z, v1.yz)
   float p4[4] = {x0, y0, z0, 1.0f};
   if (!fc.model_identity) {
@@ -138,7 +152,6 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
               b23 = -C32 * y * (4.0f * zz - xx - yy);
   const float b30 = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), b31 = -C32 * x * (4.0f * zz - xx - yy),
               b32 = C34 * z * (xx - yy), b33 = -C30 * x * (xx - 3.0f * yy);
-  const uint4* shv = reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)id);
   const float4* sh32 = SH32 ? reinterpret_cast<const float4*>(a.sh32 + 48 * (size_t)id) : nullptr;
   float color[3];
 #pragma unroll
@@ -151,8 +164,8 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
         g[4 * k] = v.x, g[4 * k + 1] = v.y, g[4 * k + 2] = v.z, g[4 * k + 3] = v.w;
       }
     } else {
-      unpack_half8(__ldg(shv + 2 * ch), g);
-      unpack_half8(__ldg(shv + 2 * ch + 1), g + 8);
+      unpack_half8(SMEM ? shv[2 * ch] : __ldg(shv + 2 * ch), g);
+      unpack_half8(SMEM ? shv[2 * ch + 1] : __ldg(shv + 2 * ch + 1), g + 8);
     }
     const float col = ((dot4(b00, b01, b02, b03, g[0], g[1], g[2], g[3]) +
                         dot4(b10, b11, b12, b13, g[4], g[5], g[6], g[7])) +
@@ -160,7 +173,6 @@ __device__ void project_splat(const FrameConst& fc, const CullArgs& a, u32 id, f
                       dot4(b30, b31, b32, b33, g[12], g[13], g[14], g[15]);
     color[ch] = fmaxf(col + 0.5f, 0.0f);
   }
-  const float o = __ldg(a.opacity + id);
 
   const float m00 = ct / s0, m01 = st / s0, m10 = -st / s1, m11 = ct / s1;
   const bool drawn = (s1 > 0.0f) && isfinite(m00) && isfinite(m01) && isfinite(m10) && isfinite(m11) &&
@@ -254,6 +266,222 @@ __global__ __launch_bounds__(kCullThreads, 6) void k_cull_project(const FrameCon
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+// The same pass with the splat buffers streamed into shared memory by the Tensor Memory Accelerator.
+// Partitions of kStreamSplats splats (one per compute thread); each CTA keeps two partitions in
+// flight: while it culls, projects and compacts one, the bulk copies (cp.async.bulk, completion counted
+// in bytes on an mbarrier) of the next land in the other stage.  The copies move every byte of the
+// partition's position, cov3d, opacity and SH rows -- also those of splats that turn out invisible,
+// whose sectors DRAM delivers anyway when the per-thread loads skip them -- so the scene streams at the
+// copy engine's rate with no registers held for loads in flight.  Arithmetic and outputs are those of
+// k_cull_project (the same device functions), bit for bit.  The last partition, when partial, is
+// loaded by the threads (its byte counts need not be multiples of 16).
+//
+// Warp specialisation: eight compute warps and a control warp.  The control warp takes the tickets,
+// arms and issues the bulk copies, publishes each partition's count and resolves the look-back of the
+// PREVIOUS partition while the compute warps project the current one; the compute warps write a
+// partition's keys and ids one iteration later, once its offset is known.  Nothing on the compute
+// warps' path waits for another CTA.
+constexpr u32 kStreamSplats = 256;
+constexpr u32 kStreamThreads = kStreamSplats + 32;
+struct StreamStage {
+  float pos[kStreamSplats * 3];
+  float cov[kStreamSplats * 6];
+  float opa[kStreamSplats];
+  uint4 sh[kStreamSplats * 6];
+};
+constexpr u32 kStageBytes = (u32)sizeof(StreamStage);
+static_assert(kStageBytes == kStreamSplats * (12 + 24 + 4 + 96), "stage layout");
+static_assert(kStreamSplats == kCullStatusSplats, "one look-back status word per partition");
+constexpr u32 kStreamSmem = 2 * kStageBytes;
+// resident CTAs per SM the grid is sized for (at most 3 fit the shared memory)
+#ifndef GS_STREAM_CTAS_PER_SM
+#define GS_STREAM_CTAS_PER_SM 3
+#endif
+constexpr u32 kStreamCtasPerSm = GS_STREAM_CTAS_PER_SM;
+
+__device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, u32 bytes, u64* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Waits (bounded) for phase `parity` of the barrier; false when the wait gave up.
+__device__ __forceinline__ bool mbar_wait(u64* bar, u32 parity) {
+  for (u32 spin = 0; spin < kMaxSpins; ++spin) {
+    u32 done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void compute_bar() {  // the compute warps only (named barrier 1)
+  asm volatile("bar.sync 1, %0;" ::"n"(kStreamSplats) : "memory");
+}
+
+__global__ __launch_bounds__(kStreamThreads, 3) void k_cull_stream(const FrameConst fc, const CullArgs a) {
+  extern __shared__ __align__(128) unsigned char s_dyn[];
+  StreamStage* stage = reinterpret_cast<StreamStage*>(s_dyn);
+  constexpr u32 kW = kStreamSplats / 32;  // compute warps
+  __shared__ u64 s_bar[2];
+  __shared__ u32 s_ticket[2];
+  __shared__ u32 s_cnt[2][kW], s_off[2][kW];
+  __shared__ u32 s_key[2][kStreamSplats];
+  __shared__ u32 s_acc[2], s_base[2], s_abort;
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const bool control = warp == kW;
+  const u32 n = fc.n;
+  const u32 nparts = (n + kStreamSplats - 1) / kStreamSplats;
+  const bool partial_tail = (n % kStreamSplats) != 0;
+
+  // control lane 0: the four bulk copies of partition p into stage s (none for a partial last partition)
+  const auto issue = [&](u32 s, u32 p) {
+    if (p >= nparts || (partial_tail && p == nparts - 1)) return;
+    const size_t b = (size_t)p * kStreamSplats;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage's earlier reads come first
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&s_bar[s])),
+                 "r"(kStageBytes)
+                 : "memory");
+    bulk_copy_g2s(stage[s].pos, a.position + 3 * b, kStreamSplats * 12, &s_bar[s]);
+    bulk_copy_g2s(stage[s].cov, a.cov3d + 6 * b, kStreamSplats * 24, &s_bar[s]);
+    bulk_copy_g2s(stage[s].opa, a.opacity + b, kStreamSplats * 4, &s_bar[s]);
+    bulk_copy_g2s(stage[s].sh, a.sh + 48 * b, kStreamSplats * 96, &s_bar[s]);
+  };
+  // the control warp: the offset of partition q (stage qs) from the look-back
+  const auto resolve = [&](u32 q, u32 qs) {
+    const u32 acc = s_acc[qs];
+    const u32 excl = lb_resolve_warp(a.status, 1, q, a.epoch, acc, a.err);
+    if (lane == 0) {
+      s_base[qs] = excl;
+      if (q == nparts - 1) *a.visible_count = excl + acc;
+    }
+  };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+    s_ticket[0] = atomicAdd(a.ticket, 1u);
+    s_ticket[1] = atomicAdd(a.ticket, 1u);
+    issue(0, s_ticket[0]);
+    issue(1, s_ticket[1]);
+  }
+  __syncthreads();
+  u32 parity = 0;  // bit s: the phase stage s waits for next
+  const u32 ltm = lanemask_lt();
+  bool have_prev = false, vis_prev = false;
+  u32 q = 0, ball_prev = 0, s = 0;
+  for (;; s ^= 1u) {
+    const u32 p = s_ticket[s];
+    if (p >= nparts) break;
+    const u32 base = p * kStreamSplats;
+    const bool tail = partial_tail && p == nparts - 1;
+    StreamStage& st = stage[s];
+    bool vis = false;
+    u32 ball = 0;
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+    if (!control) {
+      if (tail) {
+        const u32 cnt = n - base;
+        for (u32 i = tid; i < 3 * cnt; i += kStreamSplats) st.pos[i] = __ldg(a.position + 3 * (size_t)base + i);
+        for (u32 i = tid; i < 6 * cnt; i += kStreamSplats) st.cov[i] = __ldg(a.cov3d + 6 * (size_t)base + i);
+        for (u32 i = tid; i < cnt; i += kStreamSplats) st.opa[i] = __ldg(a.opacity + base + i);
+        const uint4* shg = reinterpret_cast<const uint4*>(a.sh + 48 * (size_t)base);
+        for (u32 i = tid; i < 6 * cnt; i += kStreamSplats) st.sh[i] = __ldg(shg + i);
+        compute_bar();
+      } else if (!mbar_wait(&s_bar[s], (parity >> s) & 1u)) {
+        atomicOr(&s_abort, 1u);
+      }
+      const u32 id = base + tid;
+      if (id < n) {
+        x = st.pos[3 * tid + 0];
+        y = st.pos[3 * tid + 1];
+        z = st.pos[3 * tid + 2];
+        const float v[4] = {x, y, z, 1.0f};
+        float c[4];
+        mat4_vec4(fc.pvm, v, c);
+        const float cx = c[0] / c[3], cy = c[1] / c[3], cz = c[2] / c[3];
+        vis = fabsf(cx) <= 1.0f && fabsf(cy) <= 1.0f && cz >= 0.0f && cz <= 1.0f;
+        s_key[s][tid] = __float_as_uint(1.0f - cz);
+      }
+      ball = __ballot_sync(0xffffffffu, vis);
+      if (lane == 0) s_cnt[s][warp] = __popc(ball);
+    }
+    if (!tail) parity ^= 1u << s;
+    __syncthreads();  // A: the partition is culled
+    if (s_abort) {  // a stage's copies never completed: record it, give the copies in flight a last
+                    // bounded wait, and leave
+      if (tid == 0) {
+        atomicOr(a.err, ERR_TIMEOUT);
+        mbar_wait(&s_bar[s], ((parity >> s) & 1u) ^ 1u);
+        const u32 other = s_ticket[s ^ 1u];
+        if (other < nparts && !(partial_tail && other == nparts - 1))
+          mbar_wait(&s_bar[s ^ 1u], (parity >> (s ^ 1u)) & 1u);
+      }
+      return;
+    }
+    if (control) {
+      if (lane == 0) {  // publish this partition's count at once
+        u32 acc = 0;
+        for (u32 w = 0; w < kW; ++w) {
+          s_off[s][w] = acc;
+          acc += s_cnt[s][w];
+        }
+        s_acc[s] = acc;
+        lb_publish(a.status, 1, p, a.epoch, acc);
+      }
+      __syncwarp();
+      if (have_prev) resolve(q, s ^ 1u);  // overlaps the projection below
+    } else if (vis) {
+      const float* cv = st.cov + 6 * tid;
+      project_values<false, true>(fc, a, base + tid, x, y, z, cv[0], cv[1], cv[2], cv[3], cv[4], cv[5],
+                                  st.sh + 6 * tid, st.opa[tid]);
+    }
+    __syncthreads();  // B: the stage is read and the previous partition's offset is known
+    if (control) {
+      if (lane == 0) {
+        const u32 next = atomicAdd(a.ticket, 1u);
+        s_ticket[s] = next;
+        issue(s, next);
+      }
+    } else if (have_prev && vis_prev) {
+      const u32 qs = s ^ 1u;
+      const u32 slot = s_base[qs] + s_off[qs][warp] + __popc(ball_prev & ltm);
+      a.key[slot] = s_key[qs][tid];
+      a.index[slot] = q * kStreamSplats + tid;
+    }
+    have_prev = true;
+    q = p;
+    vis_prev = vis;
+    ball_prev = ball;
+  }
+  if (!have_prev) return;
+  if (control) resolve(q, s ^ 1u);  // the last partition of this CTA
+  __syncthreads();
+  if (!control && vis_prev) {
+    const u32 qs = s ^ 1u;
+    const u32 slot = s_base[qs] + s_off[qs][warp] + __popc(ball_prev & ltm);
+    a.key[slot] = s_key[qs][tid];
+    a.index[slot] = q * kStreamSplats + tid;
+  }
+}
+
+bool cull_stream_usable(const CullArgs& a) {
+  const auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  return !a.sh32 && aligned(a.position) && aligned(a.cov3d) && aligned(a.opacity) && aligned(a.sh);
+}
+
+cudaError_t cull_stream_init() {
+  return cudaFuncSetAttribute(k_cull_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamSmem);
 }
 
 // Many views of the same splats in one pass (the batched form): each partition's positions are loaded
@@ -376,12 +604,19 @@ cudaError_t launch_cull_views(const CullViewsArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-const void* cull_project_kernel() { return reinterpret_cast<const void*>(&k_cull_project<false>); }
+bool is_cull_kernel(const void* f) {
+  return f == reinterpret_cast<const void*>(&k_cull_project<false>) || f == reinterpret_cast<const void*>(&k_cull_stream);
+}
 
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream) {
   if (fc.n == 0) return cudaSuccess;
-  const u32 parts = (fc.n + kCullTile - 1) / kCullTile;
   const int sms = a.num_sms > 0 ? a.num_sms : 1;
+  if (a.staged && cull_stream_usable(a)) {
+    const u32 parts = (fc.n + kStreamSplats - 1) / kStreamSplats;
+    k_cull_stream<<<min(parts, (u32)sms * kStreamCtasPerSm), kStreamThreads, kStreamSmem, stream>>>(fc, a);
+    return cudaGetLastError();
+  }
+  const u32 parts = (fc.n + kCullTile - 1) / kCullTile;
   const u32 grid = min(parts, (u32)sms * 8u);
   if (a.sh32)
     k_cull_project<true><<<grid, kCullThreads, 0, stream>>>(fc, a);

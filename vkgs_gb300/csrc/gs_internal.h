@@ -58,6 +58,7 @@ struct CullArgs {
   u32 epoch;
   u32* err;
   int num_sms;
+  int staged;        // nonzero: the shared-memory-staged kernel (when the buffers allow its bulk copies)
 };
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
 
@@ -86,7 +87,9 @@ struct CullViewsArgs {
   CullView view[kMaxCullViews];
 };
 cudaError_t launch_cull_views(const CullViewsArgs& a, cudaStream_t stream);
-const void* cull_project_kernel();  // the plain path's cull kernel (the only one reading the camera)
+bool is_cull_kernel(const void* f);  // the plain path's cull kernels (the only ones reading the camera)
+cudaError_t cull_stream_init();     // opts the shared-memory-staged cull into its dynamic shared memory
+constexpr u32 kCullStatusSplats = 256;  // splats per look-back status word of the plain cull (its finest partition)
 
 // Gathers instance records into sorted order and writes the indirect draw arguments.
 cudaError_t launch_instances(const u32* index, const u32* visible_count, const float* inst_by_id, u32 n,
