@@ -211,9 +211,9 @@ gs_status gs_render(gs_context* context, const gs_splats* splats, const gs_camer
 /* No counterpart in the reference (its viewer renders one camera per frame).  Renders n_views cameras
  * of the same splats, view v into targets[v] (sizes may differ; each within the context's maxima), as
  * gs_render would one by one.  With render lanes (gs_context_set_batch_lanes), one cull + projection
- * pass over the splats serves up to 32 views at a time (each splat's data is read once for all of
- * them; per-view outputs identical to gs_render's), then each view's depth sort, binning and raster
- * run on a lane: sub-contexts with their own scratch and stream, forked from `stream` and joined back
+ * pass over the splats serves 8 views at a time (each splat's data is read once for all of them;
+ * per-view outputs identical to gs_render's), largest views first, and each view's depth sort, binning
+ * and raster run on a lane as soon as its pass is done (the later passes overlap the lanes' work): sub-contexts with their own scratch and stream, forked from `stream` and joined back
  * into it with events, so the batch is ordered on `stream` and can be captured in a CUDA graph as a
  * whole.  The shared pass keeps every view's records (72 bytes per splat and view, at most 64 views
  * at a time) in an arena allocated by the first batched call that needs it.  A later call that needs

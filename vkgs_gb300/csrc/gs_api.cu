@@ -125,6 +125,7 @@ struct gs_context {
   cudaStream_t lane_stream[GS_MAX_LANES] = {};
   cudaEvent_t lane_join[GS_MAX_LANES] = {};
   cudaEvent_t batch_fork = nullptr;
+  cudaEvent_t chunk_done[64] = {};  // batched render: one per shared-cull chunk (kMaxBatchViews / kCullChunk)
   u32 nlanes = 0;
   bool last_batched = false;
   u32 slab_count = 2;  // nearest eighth of the visible splats, then the rest
@@ -440,6 +441,10 @@ static void destroy_lanes(gs_context* c) {
   }
   if (c->batch_fork) cudaEventDestroy(c->batch_fork);
   c->batch_fork = nullptr;
+  for (cudaEvent_t& e : c->chunk_done) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   c->nlanes = 0;
 }
 
@@ -886,6 +891,8 @@ static gs_status join_lanes(gs_context* c, u32 used, cudaStream_t st) {
 // its compacted keys, ids and records.  Allocated by the first batched call that needs them (never
 // while the stream is being captured: that call takes the per-lane cull instead).
 constexpr u32 kMaxBatchViews = 64;
+constexpr u32 kCullChunk = 8;  // views per shared-cull launch of the batched render (pipelined with the lanes)
+static_assert(kMaxBatchViews / kCullChunk <= 64 && kCullChunk <= kMaxCullViews, "chunk events and launches");
 
 struct BatchLayout {
   size_t status_off, head_bytes, status_words, view_stride, key_off, index_off, record_off, total;
@@ -895,7 +902,7 @@ static BatchLayout batch_layout(u32 views, u32 n) {
   BatchLayout b{};
   const auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   b.status_words = (n + kCullTile - 1) / kCullTile;
-  b.status_off = up((size_t)(kMaxBatchViews + kMaxBatchViews / kMaxCullViews + 1) * sizeof(u32));
+  b.status_off = up((size_t)(2 * kMaxBatchViews + 1) * sizeof(u32));  // visible words, tickets
   b.head_bytes = b.status_off + up((size_t)views * b.status_words * sizeof(u64));
   b.key_off = 0;
   b.index_off = up((size_t)n * sizeof(u32));
@@ -939,67 +946,99 @@ static PreCulled batch_slot(const gs_context* c, u32 w) {
 
 // The cull + projection of cams[0 .. nv) (nv <= batch_views) into arena slots 0 .. nv-1, k_cull_views
 // launches of up to kMaxCullViews views on `st`.  sh32: FP32 SH (the differentiable path).
-static gs_status shared_cull(gs_context* c, const gs_splats* s, const float* sh32, u32 nv, const gs_camera* cams,
-                             cudaStream_t st) {
+// Clears the arena's head (visible words, tickets, look-back status) before a batch's culls.
+static gs_status batch_head_clear(gs_context* c, cudaStream_t st) {
+  const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
+  ++c->batch_gen;
+  return cudaMemsetAsync(c->batch_arena, 0, b.head_bytes, st) == cudaSuccess ? GS_SUCCESS : GS_ERROR_CUDA;
+}
+
+// One k_cull_views launch (cnt <= kMaxCullViews views) into arena slots slots[0 .. cnt), cams[slot] being
+// the slot's camera, with launch ticket `ticket` of the batch.  sh32: FP32 SH (the differentiable path).
+static gs_status cull_views_launch(gs_context* c, const gs_splats* s, const float* sh32, const u32* slots, u32 cnt,
+                                   const gs_camera* cams, u32 ticket, cudaStream_t st) {
   const BatchLayout b = batch_layout(c->batch_views, c->batch_n);
   char* base = c->batch_arena;
-  ++c->batch_gen;
   u32* tickets = reinterpret_cast<u32*>(base) + kMaxBatchViews;
   u64* status = reinterpret_cast<u64*>(base + b.status_off);
-  if (cudaMemsetAsync(base, 0, b.head_bytes, st) != cudaSuccess) return GS_ERROR_CUDA;
   std::unique_ptr<CullViewsArgs> ca(new CullViewsArgs{});
-  for (u32 c0 = 0; c0 < nv; c0 += kMaxCullViews) {
-    const u32 cnt = std::min(kMaxCullViews, nv - c0);
-    ca->position = s->position;
-    ca->cov3d = s->cov3d;
-    ca->opacity = s->opacity;
-    ca->sh = s->sh;
-    ca->sh32 = sh32;
-    ca->n = s->count;
-    ca->count = cnt;
-    ca->ticket = tickets + c0 / kMaxCullViews;
-    ca->epoch = 1;
-    ca->err = c->err;
-    ca->num_sms = c->num_sms;
-    for (u32 i = 0; i < cnt; ++i) {
-      const u32 w = c0 + i;
-      const gs_camera& cam = cams[w];
-      frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, s->count,
-                      &ca->fc[i]);
-      const PreCulled pre = batch_slot(c, w);
-      ca->view[i] = CullView{pre.key, pre.index, pre.record, pre.visible, status + (size_t)w * b.status_words};
-    }
-    if (launch_cull_views(*ca, st) != cudaSuccess) return GS_ERROR_CUDA;
+  ca->position = s->position;
+  ca->cov3d = s->cov3d;
+  ca->opacity = s->opacity;
+  ca->sh = s->sh;
+  ca->sh32 = sh32;
+  ca->n = s->count;
+  ca->count = cnt;
+  ca->ticket = tickets + ticket;
+  ca->epoch = 1;
+  ca->err = c->err;
+  ca->num_sms = c->num_sms;
+  for (u32 i = 0; i < cnt; ++i) {
+    const u32 w = slots[i];
+    const gs_camera& cam = cams[w];
+    frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, s->count,
+                    &ca->fc[i]);
+    const PreCulled pre = batch_slot(c, w);
+    ca->view[i] = CullView{pre.key, pre.index, pre.record, pre.visible, status + (size_t)w * b.status_words};
   }
-  return GS_SUCCESS;
+  return launch_cull_views(*ca, st) == cudaSuccess ? GS_SUCCESS : GS_ERROR_CUDA;
+}
+
+// The cull + projection of cams[0 .. nv) (nv <= batch_views) into arena slots 0 .. nv-1, k_cull_views
+// launches of up to kMaxCullViews views on `st`.  sh32: FP32 SH (the differentiable path).
+static gs_status shared_cull(gs_context* c, const gs_splats* s, const float* sh32, u32 nv, const gs_camera* cams,
+                             cudaStream_t st) {
+  gs_status r = batch_head_clear(c, st);
+  u32 slots[kMaxCullViews];
+  for (u32 c0 = 0; r == GS_SUCCESS && c0 < nv; c0 += kMaxCullViews) {
+    const u32 cnt = std::min(kMaxCullViews, nv - c0);
+    for (u32 i = 0; i < cnt; ++i) slots[i] = c0 + i;
+    r = cull_views_launch(c, s, sh32, slots, cnt, cams, c0 / kMaxCullViews, st);
+  }
+  return r;
 }
 
 // Views [v0, v0 + nv) of the batch: their culls in k_cull_views launches on `st`, then their frames
 // from the depth sort on, spread over the lanes.
 static gs_status batched_group(gs_context* c, const gs_splats* s, u32 v0, u32 nv, const gs_camera* cams,
                                const gs_target* targets, cudaStream_t st) {
-  gs_status r = shared_cull(c, s, nullptr, nv, cams + v0, st);
-  if (r != GS_SUCCESS) return r;
-  const u32 used = std::min(c->nlanes, std::max(nv, 1u));
-  if ((r = fork_lanes(c, used, st)) != GS_SUCCESS) return r;
   // Largest views first, each to the lane with the least work so far (work ~ pixels + a fixed cost per
-  // view), so the lanes finish together.
+  // view), so the lanes finish together.  The views are culled in chunks of kCullChunk in that order,
+  // each chunk one k_cull_views launch on `st` followed by an event: a lane starts a view as soon as
+  // its chunk is culled, so the later chunks' culls overlap the lanes' sorting, binning and blending.
   std::vector<u32> order(nv);
   for (u32 w = 0; w < nv; ++w) order[w] = w;
   const auto work = [&](u32 w) { return (double)cams[v0 + w].width * cams[v0 + w].height + 250000.0; };
   std::stable_sort(order.begin(), order.end(), [&](u32 x, u32 y) { return work(x) > work(y); });
+  gs_status r = batch_head_clear(c, st);
+  if (r != GS_SUCCESS) return r;
+  const u32 used = std::min(c->nlanes, std::max(nv, 1u));
   double load[GS_MAX_LANES] = {};
-  for (u32 w : order) {
-    u32 l = 0;
-    for (u32 k = 1; k < used; ++k)
-      if (load[k] < load[l]) l = k;
-    load[l] += work(w);
-    const PreCulled pre = batch_slot(c, w);
-    r = render_frame(c->lane[l], s, nullptr, &cams[v0 + w], &targets[v0 + w], nullptr,
-                     reinterpret_cast<gs_stream>(c->lane_stream[l]), &pre);
-    if (r != GS_SUCCESS) return r;
+  bool forked[GS_MAX_LANES] = {};
+  for (u32 k0 = 0, chunk = 0; k0 < nv; k0 += kCullChunk, ++chunk) {
+    const u32 cnt = std::min(kCullChunk, nv - k0);
+    if ((r = cull_views_launch(c, s, nullptr, order.data() + k0, cnt, cams + v0, chunk, st)) != GS_SUCCESS) return r;
+    if (cudaEventRecord(c->chunk_done[chunk], st) != cudaSuccess) return GS_ERROR_CUDA;
+    for (u32 i = 0; i < cnt; ++i) {
+      const u32 w = order[k0 + i];
+      u32 l = 0;
+      for (u32 k = 1; k < used; ++k)
+        if (load[k] < load[l]) l = k;
+      load[l] += work(w);
+      if (cudaStreamWaitEvent(c->lane_stream[l], c->chunk_done[chunk], 0) != cudaSuccess) return GS_ERROR_CUDA;
+      forked[l] = true;
+      const PreCulled pre = batch_slot(c, w);
+      r = render_frame(c->lane[l], s, nullptr, &cams[v0 + w], &targets[v0 + w], nullptr,
+                       reinterpret_cast<gs_stream>(c->lane_stream[l]), &pre);
+      if (r != GS_SUCCESS) return r;
+    }
   }
-  return join_lanes(c, used, st);
+  for (u32 l = 0; l < used; ++l) {  // join the lanes that took views
+    if (!forked[l]) continue;
+    if (cudaEventRecord(c->lane_join[l], c->lane_stream[l]) != cudaSuccess) return GS_ERROR_CUDA;
+    if (cudaStreamWaitEvent(st, c->lane_join[l], 0) != cudaSuccess) return GS_ERROR_CUDA;
+  }
+  return GS_SUCCESS;
 }
 
 
@@ -1238,6 +1277,11 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
   destroy_lanes(c);
   if (lanes == 0) return GS_SUCCESS;
   if (cudaEventCreateWithFlags(&c->batch_fork, cudaEventDisableTiming) != cudaSuccess) return GS_ERROR_CUDA;
+  for (cudaEvent_t& e : c->chunk_done)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      destroy_lanes(c);
+      return GS_ERROR_CUDA;
+    }
   gs_context_options o{c->max_splats, c->max_width, c->max_height, c->pair_capacity};
   for (u32 l = 0; l < lanes; ++l) {
     gs_status st = gs_context_create(&c->lane[l], &o);
