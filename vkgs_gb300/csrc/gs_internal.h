@@ -11,7 +11,7 @@ namespace gs {
 
 // ---- radix sort (gs_sort.cu) ----
 constexpr size_t kRadixControlBytes = (4 * 256 + 4) * sizeof(uint32_t);
-constexpr u32 kRadixItems = 12;                      // keys per thread and partition
+constexpr u32 kRadixItems = 16;                      // keys per thread and partition
 constexpr u32 kRadixTile = 256 * kRadixItems;        // keys per partition
 
 struct RadixSortArgs {
