@@ -318,7 +318,9 @@ void gs_viewer_destroy(gs_viewer* viewer);
  * a slot's target must not be written by the next frame of that slot before the caller is done with it,
  * which holds when the caller's reads are enqueued on `stream` before the submit that reuses the slot.
  * gs_viewer_frame = submit + wait.  gs_viewer_check waits for every slot on `stream`, synchronises and
- * returns the first device error of the slots' contexts. */
+ * returns the first device error of the slots' contexts.  With more than one slot the frames are
+ * captured with the binning's lean launch shape (fewer count threads and emission CTAs: slower alone,
+ * more frames per second when frames overlap); render lanes use it too. */
 #define GS_MAX_FRAMES_IN_FLIGHT 8
 gs_status gs_viewer_create_frames(gs_viewer** viewer, gs_context* context, const gs_splats* splats,
                                   const gs_camera* camera, const gs_target* targets, uint32_t frames_in_flight);

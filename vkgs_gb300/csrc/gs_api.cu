@@ -69,6 +69,7 @@ struct gs_context {
   int count_fragments = 0;
   float t_floor = 1e-4f;  // early stop: remaining contributions move no channel by more than this
   bool staged_cull = false;  // plain path: stage each cull partition in shared memory with bulk copies
+  bool lean = false;         // its frames run beside other frames (viewer slots, render lanes)
   u32 epoch = 1;
   char* arena = nullptr;
   size_t arena_bytes = 0;
@@ -715,6 +716,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     ba.pair_sum = reinterpret_cast<unsigned long long*>(c->frame + FW_PAIR_SUM);
     ba.pair_peak = c->err + 1;
     ba.err = c->err;
+    ba.lean = c->lean ? 1 : 0;
     GS_TRY(launch_bin(ba, st, ev ? ev[e] : nullptr, ev ? ev[e + 1] : nullptr, c->num_sms));
     GS_MARK(e + 2);
 
@@ -1207,7 +1209,12 @@ gs_status gs_viewer_create_frames(gs_viewer** out, gs_context* c, const gs_splat
       gs_context_set_transmittance_floor(sl.ctx, c->t_floor);
       gs_context_set_cull_staging(sl.ctx, c->staged_cull);
     }
+    // With frames in flight every slot's frames run beside the others': capture them lean (the
+    // caller's own setting is restored afterwards; captured launches keep their configuration).
+    const bool lean = sl.ctx->lean;
+    sl.ctx->lean = lean || frames_in_flight > 1;
     const gs_status st = capture_slot(sl, s, cam, &targets[i]);
+    sl.ctx->lean = lean;
     if (st != GS_SUCCESS) return fail(st);
   }
   *out = v;
@@ -1297,6 +1304,7 @@ gs_status gs_context_set_batch_lanes(gs_context* c, uint32_t lanes) {
     gs_context_set_count_fragments(c->lane[l], c->count_fragments);
     gs_context_set_transmittance_floor(c->lane[l], c->t_floor);
     gs_context_set_train_slab_min(c->lane[l], c->train_slab_min);
+    c->lane[l]->lean = true;  // lanes run their views concurrently
   }
   return GS_SUCCESS;
 }

@@ -132,6 +132,7 @@ struct BinArgs {
   unsigned long long* pair_sum;  // out: sum over the frame's slabs
   u32* pair_peak;            // out: max over every slab since the context was last checked (atomicMax)
   u32* err;
+  int lean;                  // frames run concurrently: the count and emission take fewer SM slots (below)
 };
 
 size_t bin_diff_words(u32 max_tiles_x, u32 max_tiles_y);
