@@ -649,6 +649,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
   ca.err = c->err;
   ca.num_sms = c->num_sms;
   ca.staged = c->staged_cull ? 1 : 0;
+  ca.lean = c->lean ? 1 : 0;
   if (!pre) GS_TRY(launch_cull_project(fc, ca, st));
   GS_MARK(1);
 
@@ -667,6 +668,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     ra.epoch = 2;
     ra.err = c->err;
     ra.num_sms = c->num_sms;
+    ra.lean = c->lean ? 1 : 0;
     GS_TRY(radix_sort(ra, st));  // 4 passes: sorted keys/index are back in key/index
   }
 

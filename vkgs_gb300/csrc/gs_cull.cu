@@ -617,7 +617,7 @@ cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStr
     return cudaGetLastError();
   }
   const u32 parts = (fc.n + kCullTile - 1) / kCullTile;
-  const u32 grid = min(parts, (u32)sms * 8u);
+  const u32 grid = min(parts, (u32)sms * (a.lean ? kLeanCullCtasPerSm : kCullCtasPerSm));
   if (a.sh32)
     k_cull_project<true><<<grid, kCullThreads, 0, stream>>>(fc, a);
   else

@@ -174,7 +174,8 @@ cudaError_t radix_sort(const RadixSortArgs& a, cudaStream_t stream) {
   k_radix_histogram<<<hist_grid, 256, 0, stream>>>(a.keys, a.count, a.max_count, a.begin_bit, passes, hist, a.err);
   // One CTA per partition: finished CTAs free their slot for the next partition's loads, so load,
   // rank and scatter phases of different partitions overlap on every SM.
-  const u32 grid = max(1u, max_parts);
+  const u32 grid = (a.lean && kLeanSortCtasPerSm) ? max(1u, min(max_parts, (u32)sms * kLeanSortCtasPerSm))
+                                                  : max(1u, max_parts);
   u32 *ks = a.keys, *vs = a.values, *kd = a.keys_alt, *vd = a.values_alt;
   for (u32 p = 0; p < passes; ++p) {
     if (a.values)
