@@ -44,7 +44,7 @@ UNIT = "frames/s"
 OPS_PER_FRAGMENT = 20  # FP32 lane-ops per covered (pixel, splat) pair, the blend's algorithmic cost
 WORKLOAD = "large"
 DEFAULT_SLABS = 2  # the renderer's default depth-slab schedule: nearest 1/8 of the visible splats, then the rest
-FRAMES_IN_FLIGHT = 4  # viewer slots whose frames overlap on the GPU (the reference viewer keeps 2, engine.cc:743)
+FRAMES_IN_FLIGHT = 5  # viewer slots whose frames overlap on the GPU (the reference viewer keeps 2, engine.cc:743)
 
 
 def parse_args():

@@ -91,10 +91,11 @@ def test_viewer_frames_in_flight_rejects_bad_counts(cuda):
             Viewer(r, splats, cam, [torch.zeros((180, 320, 4), device="cuda")] * max(n, 1), frames_in_flight=n)
 
 
-def test_bench_viewer_four_frames_in_flight_equal_direct_renders(cuda):
+def test_bench_viewer_frames_in_flight_equal_direct_renders(cuda):
     """The headline configuration as the bench runs it: 6M splats (shell layout), 1600x900, the nine
-    cameras cycled for two laps through gs_viewer_submit with four frames in flight, the pair capacity
-    reserved from counted frames -- every frame bit-identical to a direct gs_render of its camera."""
+    cameras cycled for two laps through gs_viewer_submit with five frames in flight (lean launch shapes),
+    the pair capacity reserved from counted frames -- every frame bit-identical to a direct gs_render of
+    its camera."""
     import torch
     from vkgs_gb300 import Camera, Renderer, Viewer, parse_ply
 
@@ -110,12 +111,13 @@ def test_bench_viewer_four_frames_in_flight_equal_direct_renders(cuda):
     pairs = max(r.render_checked(splats, c)[1]["tile_pairs"] for c in cams)
     r.count_fragments(False)
     r.reserve(max_tile_pairs=int(pairs * 1.05) + 1024)
-    v = Viewer(r, splats, cams[0], torch.zeros((900, 1600, 4), device="cuda"), frames_in_flight=4)
+    slots = 5
+    v = Viewer(r, splats, cams[0], torch.zeros((900, 1600, 4), device="cuda"), frames_in_flight=slots)
     # as the bench's end-to-end loop: a slot's image is copied on a side stream after its frame, and the
-    # slot is drawn into again only after that copy, so up to four frames overlap on the GPU
+    # slot is drawn into again only after that copy, so up to five frames overlap on the GPU
     main = torch.cuda.current_stream()
     copier = torch.cuda.Stream()
-    copied = [torch.cuda.Event() for _ in range(4)]
+    copied = [torch.cuda.Event() for _ in range(slots)]
     started, got = set(), []
     for k in range(2 * len(cams)):
         slot = v.next_slot

@@ -845,6 +845,12 @@ static gs_status project_backward(gs_context* const* ctx, const gs_camera* cams,
     frame_constants(cam.projection, cam.view, cam.model, cam.camera_position, cam.width, cam.height, p->count,
                     &tv->fc[v]);
     tv->grad_rec[v] = ctx[v]->grad_rec;
+    for (int r = 0; r < 4; ++r)  // column-major inputs: element (r, c) of a matrix m is m[4 c + r]
+      for (int c = 0; c < 4; ++c) {
+        double acc = 0.0;
+        for (int k = 0; k < 4; ++k) acc += (double)cam.view[4 * k + r] * (double)cam.model[4 * c + k];
+        tv->vm[v][4 * r + c] = (float)acc;
+      }
   }
   TrainArgs ta{};
   ta.means = p->means;

@@ -209,6 +209,7 @@ struct TrainViews {
   u32 count;
   FrameConst fc[kMaxTrainViews];
   const float* grad_rec[kMaxTrainViews];
+  float vm[kMaxTrainViews][16];  // view * model, row-major (row r, column c at [4 r + c])
 };
 // Adds the raw-parameter gradients of all views into a.g_* (one kernel: no atomics).
 cudaError_t launch_project_backward(const TrainViews& views, const TrainArgs& a, cudaStream_t stream);

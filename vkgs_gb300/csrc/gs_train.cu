@@ -45,35 +45,52 @@ cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// Degree-3 SH basis B_k(d) and its gradient, the reference's coefficient order (projection.comp:140-163).
-__device__ __forceinline__ void sh_basis_grad(float x, float y, float z, float B[16], float dB[16][3]) {
+// Degree-3 SH basis B_k(d), the reference's coefficient order (projection.comp:140-163).
+__device__ __forceinline__ void sh_basis(float x, float y, float z, float B[16]) {
   const float C0 = 0.28209479177387814f, C1 = 0.4886025119029199f, C20 = 1.0925484305920792f,
               C21 = 0.31539156525252005f, C22 = 0.5462742152960396f, C30 = 0.5900435899266435f,
               C31 = 2.890611442640554f, C32 = 0.4570457994644658f, C33 = 0.3731763325901154f,
               C34 = 1.445305721320277f;
   const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
   B[0] = C0;
-  dB[0][0] = dB[0][1] = dB[0][2] = 0.0f;
-  B[1] = -C1 * y, dB[1][0] = 0.0f, dB[1][1] = -C1, dB[1][2] = 0.0f;
-  B[2] = C1 * z, dB[2][0] = 0.0f, dB[2][1] = 0.0f, dB[2][2] = C1;
-  B[3] = -C1 * x, dB[3][0] = -C1, dB[3][1] = 0.0f, dB[3][2] = 0.0f;
-  B[4] = C20 * xy, dB[4][0] = C20 * y, dB[4][1] = C20 * x, dB[4][2] = 0.0f;
-  B[5] = -C20 * yz, dB[5][0] = 0.0f, dB[5][1] = -C20 * z, dB[5][2] = -C20 * y;
-  B[6] = C21 * (2.0f * zz - xx - yy), dB[6][0] = -2.0f * C21 * x, dB[6][1] = -2.0f * C21 * y, dB[6][2] = 4.0f * C21 * z;
-  B[7] = -C20 * xz, dB[7][0] = -C20 * z, dB[7][1] = 0.0f, dB[7][2] = -C20 * x;
-  B[8] = C22 * (xx - yy), dB[8][0] = 2.0f * C22 * x, dB[8][1] = -2.0f * C22 * y, dB[8][2] = 0.0f;
-  B[9] = -C30 * y * (3.0f * xx - yy), dB[9][0] = -6.0f * C30 * xy, dB[9][1] = -C30 * (3.0f * xx - 3.0f * yy),
-  dB[9][2] = 0.0f;
-  B[10] = C31 * xy * z, dB[10][0] = C31 * yz, dB[10][1] = C31 * xz, dB[10][2] = C31 * xy;
-  B[11] = -C32 * y * (4.0f * zz - xx - yy), dB[11][0] = 2.0f * C32 * xy, dB[11][1] = -C32 * (4.0f * zz - xx - 3.0f * yy),
-  dB[11][2] = -8.0f * C32 * yz;
-  B[12] = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy), dB[12][0] = -6.0f * C33 * xz, dB[12][1] = -6.0f * C33 * yz,
-  dB[12][2] = C33 * (6.0f * zz - 3.0f * xx - 3.0f * yy);
-  B[13] = -C32 * x * (4.0f * zz - xx - yy), dB[13][0] = -C32 * (4.0f * zz - 3.0f * xx - yy), dB[13][1] = 2.0f * C32 * xy,
-  dB[13][2] = -8.0f * C32 * xz;
-  B[14] = C34 * z * (xx - yy), dB[14][0] = 2.0f * C34 * xz, dB[14][1] = -2.0f * C34 * yz, dB[14][2] = C34 * (xx - yy);
-  B[15] = -C30 * x * (xx - 3.0f * yy), dB[15][0] = -C30 * (3.0f * xx - 3.0f * yy), dB[15][1] = 6.0f * C30 * xy,
-  dB[15][2] = 0.0f;
+  B[1] = -C1 * y;
+  B[2] = C1 * z;
+  B[3] = -C1 * x;
+  B[4] = C20 * xy;
+  B[5] = -C20 * yz;
+  B[6] = C21 * (2.0f * zz - xx - yy);
+  B[7] = -C20 * xz;
+  B[8] = C22 * (xx - yy);
+  B[9] = -C30 * y * (3.0f * xx - yy);
+  B[10] = C31 * xy * z;
+  B[11] = -C32 * y * (4.0f * zz - xx - yy);
+  B[12] = C33 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+  B[13] = -C32 * x * (4.0f * zz - xx - yy);
+  B[14] = C34 * z * (xx - yy);
+  B[15] = -C30 * x * (xx - 3.0f * yy);
+}
+
+// g = sum_k W[k] dB_k/dd: the gradient of the basis contracted with per-coefficient weights, each
+// term's partial derivatives written out (no 16 x 3 table is held).
+__device__ __forceinline__ void sh_grad_dot(float x, float y, float z, const float W[16], float g[3]) {
+  const float C1 = 0.4886025119029199f, C20 = 1.0925484305920792f, C21 = 0.31539156525252005f,
+              C22 = 0.5462742152960396f, C30 = 0.5900435899266435f, C31 = 2.890611442640554f,
+              C32 = 0.4570457994644658f, C33 = 0.3731763325901154f, C34 = 1.445305721320277f;
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  float gx = -C1 * W[3], gy = -C1 * W[1], gz = C1 * W[2];
+  gx += C20 * y * W[4], gy += C20 * x * W[4];
+  gy += -C20 * z * W[5], gz += -C20 * y * W[5];
+  gx += -2.0f * C21 * x * W[6], gy += -2.0f * C21 * y * W[6], gz += 4.0f * C21 * z * W[6];
+  gx += -C20 * z * W[7], gz += -C20 * x * W[7];
+  gx += 2.0f * C22 * x * W[8], gy += -2.0f * C22 * y * W[8];
+  gx += -6.0f * C30 * xy * W[9], gy += -C30 * (3.0f * xx - 3.0f * yy) * W[9];
+  gx += C31 * yz * W[10], gy += C31 * xz * W[10], gz += C31 * xy * W[10];
+  gx += 2.0f * C32 * xy * W[11], gy += -C32 * (4.0f * zz - xx - 3.0f * yy) * W[11], gz += -8.0f * C32 * yz * W[11];
+  gx += -6.0f * C33 * xz * W[12], gy += -6.0f * C33 * yz * W[12], gz += C33 * (6.0f * zz - 3.0f * xx - 3.0f * yy) * W[12];
+  gx += -C32 * (4.0f * zz - 3.0f * xx - yy) * W[13], gy += 2.0f * C32 * xy * W[13], gz += -8.0f * C32 * xz * W[13];
+  gx += 2.0f * C34 * xz * W[14], gy += -2.0f * C34 * yz * W[14], gz += C34 * (xx - yy) * W[14];
+  gx += -C30 * (3.0f * xx - 3.0f * yy) * W[15], gy += 6.0f * C30 * xy * W[15];
+  g[0] = gx, g[1] = gy, g[2] = gz;
 }
 
 // m (column-major 4x4) as a row-major 3x3 / 4x4 element
@@ -128,32 +145,22 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
         pos[0] = a.means[3 * id], pos[1] = a.means[3 * id + 1], pos[2] = a.means[3 * id + 2];
       }
       const FrameConst& fc = vs.fc[v];
+      const float* vm = vs.vm[v];  // V M, row-major; its 3 x 3 block is A = V3 M3
       // ---- forward quantities of this view (projection.comp:95-137)
-      float A[3][3];  // V3 M3
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          A[r][c] = mel(fc.view, r, 0) * mel(fc.model, 0, c) + mel(fc.view, r, 1) * mel(fc.model, 1, c) +
-                    mel(fc.view, r, 2) * mel(fc.model, 2, c);
-      float p1[4], pv[4];
+      const auto A = [&](int r, int c) { return vm[4 * r + c]; };
+      float pv[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r)
-        p1[r] = mel(fc.model, r, 0) * pos[0] + mel(fc.model, r, 1) * pos[1] + mel(fc.model, r, 2) * pos[2] +
-                mel(fc.model, r, 3);
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-        pv[r] = mel(fc.view, r, 0) * p1[0] + mel(fc.view, r, 1) * p1[1] + mel(fc.view, r, 2) * p1[2] +
-                mel(fc.view, r, 3) * p1[3];
+        pv[r] = vm[4 * r + 0] * pos[0] + vm[4 * r + 1] * pos[1] + vm[4 * r + 2] * pos[2] + vm[4 * r + 3];
       float Cv[3][3], T3[3][3];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) T3[r][c] = A[r][0] * Sg[0][c] + A[r][1] * Sg[1][c] + A[r][2] * Sg[2][c];
+        for (int c = 0; c < 3; ++c) T3[r][c] = A(r, 0) * Sg[0][c] + A(r, 1) * Sg[1][c] + A(r, 2) * Sg[2][c];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) Cv[r][c] = T3[r][0] * A[c][0] + T3[r][1] * A[c][1] + T3[r][2] * A[c][2];
+        for (int c = 0; c < 3; ++c) Cv[r][c] = T3[r][0] * A(c, 0) + T3[r][1] * A(c, 1) + T3[r][2] * A(c, 2);
       const float x = pv[0], y = pv[1], z = pv[2];
       const float J[2][3] = {{-1.0f / z, 0.0f, x / z / z}, {0.0f, -1.0f / z, y / z / z}};
       float JC[2][3], C2[2][2];
@@ -193,11 +200,14 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
       const float dv[3] = {pos[0] - fc.cam_m[0], pos[1] - fc.cam_m[1], pos[2] - fc.cam_m[2]};
       const float dl = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
       const float dir[3] = {dv[0] / dl, dv[1] / dl, dv[2] / dl};
-      float B[16], dB[16][3];
-      sh_basis_grad(dir[0], dir[1], dir[2], B, dB);
+      float B[16];
+      sh_basis(dir[0], dir[1], dir[2], B);
 
-      // ---- colour -> SH and view direction (one channel's 16 coefficients at a time)
-      float gdir[3] = {0.0f, 0.0f, 0.0f};
+      // ---- colour -> SH and view direction (one channel's 16 coefficients at a time); the direction
+      // gradient sum_ch gc_ch sum_k c_ch,k dB_k is taken once from the weights W_k = sum_ch gc_ch c_ch,k
+      float W[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) W[k] = 0.0f;
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
         float c16[16];
@@ -212,13 +222,13 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
         const float gc = (col > 0.0f && col < 1.0f) ? gr[6 + ch] : 0.0f;  // max(., 0) and the target's clamp
         if (gc == 0.0f) continue;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) s_gsh[16 * ch + k][tid] += B[k] * gc;
-#pragma unroll
         for (int k = 0; k < 16; ++k) {
-          const float w = c16[k] * gc;
-          gdir[0] += w * dB[k][0], gdir[1] += w * dB[k][1], gdir[2] += w * dB[k][2];
+          s_gsh[16 * ch + k][tid] += B[k] * gc;
+          W[k] += c16[k] * gc;
         }
       }
+      float gdir[3];
+      sh_grad_dot(dir[0], dir[1], dir[2], W, gdir);
       const float dd = dir[0] * gdir[0] + dir[1] * gdir[1] + dir[2] * gdir[2];
       float gp[3] = {(gdir[0] - dir[0] * dd) / dl, (gdir[1] - dir[1] * dd) / dl, (gdir[2] - dir[2] * dd) / dl};
 
@@ -269,17 +279,17 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
                   mel(fc.proj, 3, c) * gpc[3];
       // pv = V M pos: the linear part is A
 #pragma unroll
-      for (int c = 0; c < 3; ++c) gpos[c] += gp[c] + (A[0][c] * gpv[0] + A[1][c] * gpv[1] + A[2][c] * gpv[2]);
+      for (int c = 0; c < 3; ++c) gpos[c] += gp[c] + (A(0, c) * gpv[0] + A(1, c) * gpv[1] + A(2, c) * gpv[2]);
       float gS[3][3];  // A^T gCv A
       float tA[3][3];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) tA[r][c] = A[0][r] * gCv[0][c] + A[1][r] * gCv[1][c] + A[2][r] * gCv[2][c];
+        for (int c = 0; c < 3; ++c) tA[r][c] = A(0, r) * gCv[0][c] + A(1, r) * gCv[1][c] + A(2, r) * gCv[2][c];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) gS[r][c] = tA[r][0] * A[0][c] + tA[r][1] * A[1][c] + tA[r][2] * A[2][c];
+        for (int c = 0; c < 3; ++c) gS[r][c] = tA[r][0] * A(0, c) + tA[r][1] * A(1, c) + tA[r][2] * A(2, c);
 
       // ---- cov3d = (R S)(R S)^T -> scale, rotation -> (unnormalised) quaternion gradient
       float gR[3][3];
