@@ -43,7 +43,7 @@ METRIC = "frames/s at 6M splats 1600x900"
 UNIT = "frames/s"
 OPS_PER_FRAGMENT = 20  # FP32 lane-ops per covered (pixel, splat) pair, the blend's algorithmic cost
 WORKLOAD = "large"
-DEFAULT_SLABS = 2  # the renderer's default depth-slab schedule: nearest 1/8 of the visible splats, then the rest
+DEFAULT_SLABS = 2  # the renderer's default depth-slab schedule: nearest 3/16 of the visible splats, then the rest
 FRAMES_IN_FLIGHT = 5  # viewer slots whose frames overlap on the GPU (the reference viewer keeps 2, engine.cc:743)
 
 
@@ -838,7 +838,7 @@ def run_ours(args):
         "config": {"workload": f"{WORKLOAD}: {n} splats (70% shell r=4, 30% uniform), 1600x900, 9 cameras "
                                "(8 on an r=8 circle + 1 at r=20), SH degree 3 in binary16",
                    "parallelism": f"replicas x{world}", "l2": "inputs (816 MB) exceed L2; no flush",
-                   "depth_slabs": "nearest 128/1024 of the visible splats, then the rest",
+                   "depth_slabs": "nearest 192/1024 of the visible splats, then the rest",
                    "frames_in_flight": FRAMES_IN_FLIGHT},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 292 * lap,
                 "d2h_bytes_per_step": H * W * 16 * lap, "frames_timed": e2e_steps,

@@ -198,8 +198,8 @@ gs_status gs_context_set_count_fragments(gs_context* context, int enable);
  * every pixel's blend state from one slab to the next; a 16x16 tile whose pixels all fall below
  * the transmittance floor is finished and receives no pairs from the slabs behind.  ends[i] is the
  * cumulative share of the visible splats in slabs 0..i, in 1/1024 units, strictly increasing,
- * with ends[count-1] = 1024; {1024} is a single slab.  The image is the same for every schedule up
- * to the early stop. */
+ * with ends[count-1] = 1024; {1024} is a single slab; the default is {192, 1024}.  The image is the
+ * same for every schedule up to the early stop. */
 #define GS_MAX_SLABS 4
 gs_status gs_context_set_slabs(gs_context* context, uint32_t count, const uint32_t* ends);
 

@@ -17,7 +17,7 @@ from dataclasses import dataclass
 import torch
 
 LANES = (1, 2, 4, 8, 12, 16, 24, 32)
-SLABS = ((1024,), (128, 1024), (256, 1024))
+SLABS = ((1024,), (128, 1024), (192, 1024), (256, 1024))
 
 
 @dataclass

@@ -129,8 +129,8 @@ struct gs_context {
   cudaEvent_t chunk_done[64] = {};  // batched render: one per shared-cull chunk (kMaxBatchViews / kCullChunk)
   u32 nlanes = 0;
   bool last_batched = false;
-  u32 slab_count = 2;  // nearest eighth of the visible splats, then the rest
-  u32 slab_end[GS_MAX_SLABS] = {128, 1024, 1024, 1024};
+  u32 slab_count = 2;  // nearest 3/16 of the visible splats, then the rest
+  u32 slab_end[GS_MAX_SLABS] = {192, 1024, 1024, 1024};
   size_t status_bytes_begin = 0, status_bytes_end = 0;  // epoch-tagged region (zeroed on allocation)
   // stage timing: a ring of kTimingRing frames x kFrameEvents events -- start, after cull, after the
   // depth sort, then per slab: after binning, tile sort, tile ranges and raster
