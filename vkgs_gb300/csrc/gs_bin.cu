@@ -703,10 +703,10 @@ cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_
   const u32 tiles = a.tiles_x * a.tiles_y;
   const u32 dw = (a.tiles_x + 1) * a.tiles_y;
   // When other frames run beside this one (frames in flight, render lanes), the count and the emission
-  // are launched lean -- half the count's threads, a quarter of the emission's CTAs: alone they take
+  // are launched lean -- half the count's threads, an eighth of the emission's CTAs: alone they take
   // longer (count 0.32 vs 0.24 ms on the bench workload), but they leave SM slots to the concurrent
-  // frames, which gives more frames per second overall (with the lean cull and sort grids: 861 vs 824
-  // frames/s with four frames in flight).
+  // frames, which gives more frames per second overall (with the lean cull and sort grids: 885 vs 869
+  // frames/s with five frames in flight; 861 vs 824 with four, before the emission went 2 -> 1).
   const u32 count_threads = a.lean ? kCountThreads / 2 : kCountThreads;
   const u32 count_grid = max(1u, min((a.n + count_threads - 1) / count_threads, sms * 2u));
   if (dw <= kCountSmemWords)
@@ -716,7 +716,7 @@ cudaError_t launch_bin(const BinArgs& a, cudaStream_t stream, cudaEvent_t after_
   k_bin_giant_count<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
   k_bin_scan<<<1, 1024, 0, stream>>>(a);
   if (after_scan) cudaEventRecord(after_scan, stream);
-  const u32 emit_grid = max(1u, min((a.n + kEmitThreads - 1) / kEmitThreads, sms * (a.lean ? 2u : 8u)));
+  const u32 emit_grid = max(1u, min((a.n + kEmitThreads - 1) / kEmitThreads, sms * (a.lean ? 1u : 8u)));
   k_bin_emit<<<emit_grid, kEmitThreads, 0, stream>>>(a);
   k_bin_giant_emit<<<sms * 2u, kGiantThreads, 0, stream>>>(a);
   if (after_emit) cudaEventRecord(after_emit, stream);

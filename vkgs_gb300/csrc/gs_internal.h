@@ -29,7 +29,7 @@ struct RadixSortArgs {
   int num_sms;
   int lean;           // frames run concurrently: at most kLeanSortCtasPerSm CTAs per SM (0: one per partition)
 };
-constexpr u32 kLeanSortCtasPerSm = 2;
+constexpr u32 kLeanSortCtasPerSm = 1;
 
 u32 radix_passes(u32 begin_bit, u32 end_bit);
 size_t radix_status_words(u32 max_count);
@@ -63,7 +63,7 @@ struct CullArgs {
   int staged;        // nonzero: the shared-memory-staged kernel (when the buffers allow its bulk copies)
   int lean;          // frames run concurrently: a persistent grid of kLeanCullCtasPerSm CTAs per SM
 };
-constexpr u32 kCullCtasPerSm = 8, kLeanCullCtasPerSm = 4;
+constexpr u32 kCullCtasPerSm = 8, kLeanCullCtasPerSm = 3;
 cudaError_t launch_cull_project(const FrameConst& fc, const CullArgs& a, cudaStream_t stream);
 
 // The cull + projection of up to kMaxCullViews views of the same splats in one launch.
