@@ -351,8 +351,9 @@ def batched_differentiation_form(dev, quick: bool = False):
 
 def cull_forms(dev, quick: bool = False, n_override=None):
     """Camera 0 of the bench workload with each cull + projection form (per-thread loads, then partitions
-    staged in shared memory by bulk copies): two untimed frames each (the launches an ncu capture of this
-    mode sees), then the per-stage time of the cull over `reps` frames each, CUDA events."""
+    staged in shared memory by bulk copies) and then with the lean launch shapes of the viewer's slots
+    (gs_context_set_lean: the raster is k_raster_pairs): two untimed frames each (the launches an ncu
+    capture of this mode sees), then the per-stage times over `reps` frames each, CUDA events."""
     import torch
     from vkgs_gb300 import Camera, Renderer, parse_ply
 
@@ -363,21 +364,24 @@ def cull_forms(dev, quick: bool = False, n_override=None):
     r = Renderer(n, cam.width, cam.height)
     r.render_checked(splats, cam)
     out = {"workload": f"{WORKLOAD}: {n} splats, camera 0, {cam.width}x{cam.height}"}
-    for staged in (False, True):
+    forms = (("per_thread", False, False), ("staged", True, False), ("lean", False, True))
+    for _, staged, lean in forms:
         r.set_cull_staging(staged)
+        r.set_lean(lean)
         for _ in range(2):
             r.render(splats, cam)
         r.check()
     reps = 3 if quick else 20
-    for staged in (False, True):
+    for name, staged, lean in forms:
         r.set_cull_staging(staged)
+        r.set_lean(lean)
         r.enable_timing(True)
         for _ in range(reps):
             r.render(splats, cam)
         st = r.stage_times(reps)
         r.enable_timing(False)
-        out["staged" if staged else "per_thread"] = {"cull_project_ms": float(st[:, 0].mean()),
-                                                     "frame_ms": float(st.sum(1).mean())}
+        out[name] = {"cull_project_ms": float(st[:, 0].mean()), "raster_ms": float(st[:, 5].mean()),
+                     "frame_ms": float(st.sum(1).mean())}
     r.check()
     return out
 
@@ -671,6 +675,22 @@ def run_ours(args):
     r.enable_timing(False)
     r.set_cull_staging(False)
 
+    # The same frames with the launch shapes of the viewer's slots (gs_context_set_lean): what each of
+    # the headline's kernels costs alone (the raster is k_raster_pairs, two pixels per thread)
+    r.set_lean(True)
+    r.enable_timing(True)
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(K):
+        r.render(splats, cams[k % len(cams)], color=color)
+    e1.record()
+    torch.cuda.synchronize()
+    r.check()
+    lean_ms = e0.elapsed_time(e1) / K
+    lean_stage = r.stage_times(K)
+    r.enable_timing(False)
+    r.set_lean(False)
+
     # (splat, tile) pairs binned per camera on the timed path (depth slabs, finished tiles skipped)
     emitted = []
     for cam in cams:
@@ -800,6 +820,7 @@ def run_ours(args):
     vis = np.array([stats[c]["visible_count"] for c in cam_of], np.float64)
     raster_ms = stage[:, 5].astype(np.float64)
     achieved = float((frags * OPS_PER_FRAGMENT).sum() / (raster_ms.sum() / 1e3) / 1e12)
+    achieved_lean = float((frags * OPS_PER_FRAGMENT).sum() / (lean_stage[:, 5].astype(np.float64).sum() / 1e3) / 1e12)
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     cull_bytes = 12.0 * n + (8.0 + 188.0) * vis
     sort_bytes = 64.0 * vis
@@ -851,7 +872,11 @@ def run_ours(args):
                      "issue_active_ncu": raster_profile().get("issue_active"),
                      "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
                      "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair met front to "
-                             "back while the pixel's transmittance is >= the transmittance floor (1e-4)"},
+                             "back while the pixel's transmittance is >= the transmittance floor (1e-4)",
+                     "lean_form": {"kernel": "k_raster_pairs", "ms": float(lean_stage[:, 5].mean()),
+                                   "achieved": achieved_lean, "frac": achieved_lean / fp32_peak,
+                                   "form": "the raster of the headline's viewer slots (two pixels per thread, "
+                                           "packed FP32 blend), timed alone on the direct path"}},
         "roofline_hbm": {**hbm_stages, "peak_gbs": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "stages_ms": stage_mean,
         "dominant_stage": dominant,
@@ -878,6 +903,11 @@ def run_ours(args):
             "cull_project_gbs": float(cull_bytes.sum() / (staged_stage[:, 0].sum() / 1e3) / 1e9),
             "form": "gs_render with gs_context_set_cull_staging(1): cull partitions staged in shared memory "
                     "by bulk copies"},
+        "direct_render_lean": {
+            "frames_per_s": world / (lean_ms / 1e3), "ms_per_frame": lean_ms,
+            "stages_ms": {name: float(lean_stage[:, i].mean()) for i, name in enumerate(L.STAGES)},
+            "form": "gs_render with gs_context_set_lean(1): the launch shapes of the headline's viewer slots, "
+                    "each kernel alone"},
     }
     if not args.no_forms:
         line["batched"] = batched_form(dev, quick=args.steps < 9)

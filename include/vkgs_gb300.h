@@ -236,6 +236,15 @@ gs_status gs_render_batched(gs_context* context, const gs_splats* splats, uint32
  * buffers (otherwise the per-thread form runs); not used by the differentiable path (FP32 SH). */
 gs_status gs_context_set_cull_staging(gs_context* context, int enable);
 
+/* No counterpart in the reference.  1 = this context's frames run beside other work on the GPU (several
+ * contexts rendering on several streams at once): its kernels take launch shapes that leave SM slots to
+ * the others -- fewer CTAs per SM for the persistent cull, the onesweep passes and the pair emission,
+ * smaller count CTAs, and the raster with two pixels per thread (8x8-pixel warp blocks, the Gaussian and
+ * the blend as packed FP32 pairs), which issues fewer instructions per pixel but is slower alone.
+ * 0 (default) = shapes for a frame that has the GPU to itself.  Results are identical.  Viewer slots
+ * with more than one frame in flight and render lanes always run lean. */
+gs_status gs_context_set_lean(gs_context* context, int enable);
+
 /* Batched form: 1 (default) = the shared cull + projection pass above, 0 = each lane culls its views. */
 gs_status gs_context_set_batch_shared_cull(gs_context* context, int enable);
 

@@ -485,3 +485,33 @@ def test_staged_cull_with_unaligned_buffers_falls_back(cuda, oracle):
     r.check()
     o = render_cpu(oracle, act, c)
     assert float(np.abs(img.cpu().numpy().astype(np.float64) - o["image"]).max()) <= IMAGE_TOL
+
+
+@pytest.mark.parametrize("n,w,h,seed,layout", [(400_000, 1600, 900, 71, "shell"), (40_000, 333, 201, 72, "gaussian")])
+def test_lean_frames_equal_default_frames(cuda, oracle, n, w, h, seed, layout):
+    """gs_context_set_lean (the launch shapes of frames that run beside others: lean cull, sort and
+    emission grids, the raster with two pixels per thread in 8x8 warp blocks): the same visible set,
+    keys, order, records and fragment counts and bit-identical RGBA32F and BGRA8 images, with the early
+    stop and without it (fragment counting), with and without a caller depth target, at an odd width
+    (the last pixel pair of each row half outside the image), and within the bar of the oracle."""
+    from vkgs_gb300 import Renderer
+
+    rows = syn.splat_rows(n, seed, layout)
+    act = scenes.activated(oracle, rows)
+    c = scenes.camera(oracle, (0.4, 0.3, 6.0), width=w, height=h)
+    depth = np.random.default_rng(seed).uniform(0.975, 1.0, (h, w)).astype(np.float32)
+    for d in (None, depth):
+        for count in (False, True):
+            frames = []
+            for lean in (False, True):
+                r = Renderer(n, w, h)
+                r.set_lean(lean)
+                frames.append(render_gpu(act, c, depth=d, count_fragments=count, renderer=r, bgra=True))
+            a, b = frames
+            assert a["count"] == b["count"]
+            for k in ("key", "index", "instance", "image", "bgra", "draw"):
+                np.testing.assert_array_equal(a[k], b[k], err_msg=f"{k} depth={d is not None} count={count}")
+            assert a["fragments"] == b["fragments"]
+            assert a["stats"]["fragments_blended"] == b["stats"]["fragments_blended"]
+            o = render_cpu(oracle, act, c, depth=d)
+            assert_parity(b, o, fragments=count)

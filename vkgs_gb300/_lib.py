@@ -99,6 +99,7 @@ SIGNATURES = [
     ("gs_viewer_check", c_int, [c_void_p, c_void_p]),
     ("gs_context_set_batch_shared_cull", c_int, [c_void_p, c_int]),
     ("gs_context_set_cull_staging", c_int, [c_void_p, c_int]),
+    ("gs_context_set_lean", c_int, [c_void_p, c_int]),
     ("gs_render_batched", c_int,
      [c_void_p, POINTER(GsSplats), c_uint32, POINTER(GsCamera), POINTER(GsTarget), c_void_p]),
     ("gs_render", c_int,

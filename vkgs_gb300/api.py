@@ -260,6 +260,12 @@ class Renderer:
         alone, slower with frames in flight; same results)."""
         _check(self._lib.gs_context_set_cull_staging(self._h, int(bool(enable))), "gs_context_set_cull_staging")
 
+    def set_lean(self, enable: bool = True) -> None:
+        """Launch shapes for frames that run beside other work on the GPU (fewer SM slots per kernel,
+        the two-pixels-per-thread raster): slower alone, more frames per second when several contexts
+        render at once; same results.  Viewer slots (frames in flight) and render lanes always are."""
+        _check(self._lib.gs_context_set_lean(self._h, int(bool(enable))), "gs_context_set_lean")
+
     def set_batch_shared_cull(self, enable: bool = True) -> None:
         """Batched form: one cull + projection pass for all views (default) or one per lane."""
         _check(self._lib.gs_context_set_batch_shared_cull(self._h, int(bool(enable))), "set_batch_shared_cull")

@@ -566,6 +566,12 @@ gs_status gs_context_set_cull_staging(gs_context* c, int enable) {
   return GS_SUCCESS;
 }
 
+gs_status gs_context_set_lean(gs_context* c, int enable) {
+  if (!c) return GS_ERROR_INVALID_ARGUMENT;
+  c->lean = enable != 0;
+  return GS_SUCCESS;
+}
+
 gs_status gs_context_set_transmittance_floor(gs_context* c, float t_floor) {
   if (!c || !(t_floor > 0.0f) || !(t_floor <= 1.0f / 255.0f)) return GS_ERROR_INVALID_ARGUMENT;
   c->t_floor = t_floor;
@@ -742,6 +748,7 @@ static gs_status render_frame(gs_context* c, const gs_splats* s, const float* sh
     rr.first = k == 0;
     rr.last = k + 1 == slabs;
     rr.nproc = train ? c->train_nproc + k * pix_stride : nullptr;
+    rr.lean = c->lean ? 1 : 0;
     GS_TRY(launch_raster(rr, st));
     GS_MARK(e + 3);
   }

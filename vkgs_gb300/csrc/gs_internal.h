@@ -162,6 +162,7 @@ struct RasterArgs {
   u32* nproc;                // differentiable forward: per pixel, list entries blended (exact stop at t_floor)
   unsigned long long* fragments;  // non-null: [0] covered fragments, [1] those met while T >= t_floor
                                   // (disables the early stop)
+  int lean;                  // frames run concurrently: two pixels per thread (same results)
 };
 cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream);
 

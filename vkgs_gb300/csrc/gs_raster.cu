@@ -11,9 +11,10 @@
 // A = sum a_i^2 T_i + T_end, T_i = prod_{j nearer} (1 - a_j).  The coverage arithmetic uses
 // explicitly rounded operations (no FMA) so that the set of covered (pixel, splat) pairs is exactly
 // the restatement's.  Each warp owns an 8x4 pixel block and walks only the records whose quad can
-// reach that block (a conservative per-batch test), which leaves every pixel's sum unchanged.  A warp
-// stops once its pixels' transmittance is below t_floor, and the tile once all its pixels are: the
-// splats behind can then change no channel by more than t_floor.  The sorted splats arrive in depth
+// reach that block (a conservative per-batch test), which leaves every pixel's sum unchanged.  Each
+// pixel stops blending exactly when its transmittance falls below t_floor (the splats behind can then
+// change no channel by more than t_floor), so its sum does not depend on how pixels are grouped into
+// warps; a warp stops walking once all its pixels have stopped, and the tile once all its warps have.  The sorted splats arrive in depth
 // slabs, nearest first: a tile that is not finished stores its pixels' running sums for the next
 // slab's launch, a finished one writes its pixels and is marked done (later slabs skip it), and the
 // last slab writes every remaining tile.
@@ -35,34 +36,36 @@ static_assert(kBlockW * kBlockH == 32 && (kTile / kBlockW) * (kTile / kBlockH) =
 // rot_scale^-1 the blend evaluates, widened by a rounding margin far above the error of either
 // evaluation).  A cleared bit therefore means no pixel centre of the block is covered, and the
 // record changes none of its pixels.
+template <int BW = kBlockW, int BH = kBlockH>
 __device__ __forceinline__ u32 block_mask(const float4 q0, const float4 q1, const float4 q3, float ox, float oy,
                                           float sx, float sy, float mx, float my) {
   // ox, oy: NDC of the tile's first pixel centre; sx, sy: NDC step between pixel centres
-  const float hx = 0.5f * (kBlockW - 1) * sx, hy = 0.5f * (kBlockH - 1) * sy;  // block half extents
+  constexpr int kBX = kTile / BW;
+  const float hx = 0.5f * (BW - 1) * sx, hy = 0.5f * (BH - 1) * sy;  // block half extents
   const float ex = 3.0f * (fabsf(q3.x) + fabsf(q3.z)) + mx + hx;
   const float ey = 3.0f * (fabsf(q3.y) + fabsf(q3.w)) + my + hy;
   const float au0 = fabsf(q0.z), au1 = fabsf(q0.w), av0 = fabsf(q1.x), av1 = fabsf(q1.y);
   const float ru = au0 * hx + au1 * hy, rv = av0 * hx + av1 * hy;
   u32 m = 0;
 #pragma unroll
-  for (int by = 0; by < kTile / kBlockH; ++by) {
-    const float dy = oy + (by * kBlockH + 0.5f * (kBlockH - 1)) * sy - q0.y;
+  for (int by = 0; by < kTile / BH; ++by) {
+    const float dy = oy + (by * BH + 0.5f * (BH - 1)) * sy - q0.y;
 #pragma unroll
-    for (int bx = 0; bx < kBlocksX; ++bx) {
-      const float dx = ox + (bx * kBlockW + 0.5f * (kBlockW - 1)) * sx - q0.x;
+    for (int bx = 0; bx < kBX; ++bx) {
+      const float dx = ox + (bx * BW + 0.5f * (BW - 1)) * sx - q0.x;
       const float u = q0.z * dx + q0.w * dy, v = q1.x * dx + q1.y * dy;
       const float tu = 3.0f + ru + 4e-6f * (au0 * (fabsf(dx) + hx) + au1 * (fabsf(dy) + hy)) + 1e-3f;
       const float tv = 3.0f + rv + 4e-6f * (av0 * (fabsf(dx) + hx) + av1 * (fabsf(dy) + hy)) + 1e-3f;
       const bool hit = fabsf(dx) <= ex && fabsf(dy) <= ey && fabsf(u) <= tu && fabsf(v) <= tv;
-      m |= hit ? 1u << (by * kBlocksX + bx) : 0u;
+      m |= hit ? 1u << (by * kBX + bx) : 0u;
     }
   }
   return m;
 }
 
-// TRAIN (the differentiable forward): every pixel stops exactly when its transmittance falls below
-// t_floor and records how many list entries it blended (nproc) and its final transmittance, which is
-// all the backward needs to walk the list in reverse.
+// TRAIN (the differentiable forward): every pixel also records how many list entries it blended
+// (nproc) and its final transmittance, which is all the backward needs to walk the list in reverse.
+// COUNT blends every fragment (no stop) and counts the covered ones.
 template <bool DEPTH, bool COUNT, bool TRAIN>
 __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a) {
   __shared__ float4 s_q0[kRasterThreads];  // cx, cy, m00, m01
@@ -122,7 +125,6 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
         while (word) {
           const u32 j = 32u * k + (u32)(__ffs(word) - 1);
           word &= word - 1u;
-          if (TRAIN && T < a.t_floor) continue;  // this pixel has stopped
           const float4 q0 = s_q0[j], q1 = s_q1[j];
           const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
           const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
@@ -132,9 +134,11 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
           if (COUNT) {
             frags += (cov && inside) ? 1u : 0u;
             needed += (cov && inside && T >= a.t_floor) ? 1u : 0u;
+          } else {
+            cov &= T >= a.t_floor;  // a pixel stops exactly when its transmittance falls below t_floor
           }
-          const float g = exp2f(kExp * (u * u + v * v));
-          const float al = cov ? q1.w * g : 0.0f;
+          const float g = cov ? exp2f(__fmul_rn(__fmaf_rn(u, u, __fmul_rn(v, v)), kExp)) : 0.0f;
+          const float al = __fmul_rn(q1.w, g);
           const float w = al * T;
           const float4 q2 = s_q2[j];
           cr += w * q2.x;
@@ -184,12 +188,191 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
   }
 }
 
+// The plain and the counting forward with two horizontally adjacent pixels per thread: 128 threads
+// per tile, each warp owning an 8x8 block (4 pixel pairs x 8 rows).  A record's shared-memory loads,
+// the walk over the block's record bits and the vertical offset serve both pixels of a thread; each
+// pixel's coverage test keeps the explicitly rounded scalar operations above (the pair's dx is one
+// packed add of the negated centre, exact), so the covered set is still exactly the restatement's,
+// and the Gaussian and the blend run as packed FP32 pairs, one instruction for both pixels.  Shared
+// memory holds the values the packed operations take twice, side by side.
+constexpr int kPairThreads = kTile * kTile / 2;
+constexpr int kPairWarps = kPairThreads / 32;  // 4 blocks of 64 pixels
+constexpr int kPairBatch = 256;                // records per batch, two per thread
+constexpr int kPairWords = kPairBatch / 32;
+
+constexpr int kPairBW = 8, kPairBH = 8, kPairBX = kTile / kPairBW;  // 8x8 blocks, 2 x 2 per tile
+static_assert(kPairWarps * kPairBW * kPairBH == kTile * kTile && kPairBW * kPairBH == 64, "pair blocks");
+
+template <bool DEPTH, bool COUNT>
+__global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterArgs a) {
+  __shared__ float4 s_a[kPairBatch];  // (-cx, -cx, -cy, m00)
+  __shared__ float4 s_b[kPairBatch];  // (m01, m10, m11, z)
+  __shared__ float4 s_c[kPairBatch];  // (r, r, g, g)
+  __shared__ float4 s_d[kPairBatch];  // (b, b, opacity, opacity)
+  __shared__ u32 s_bits[kPairWarps][kPairWords];  // [block][32-record word]
+  const u32 tile = blockIdx.x;
+  if (!a.first && ((a.tile_done[tile >> 5] >> (tile & 31u)) & 1u)) return;  // finished by an earlier slab
+  const u32 tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+  const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const u32 px = tx * kTile + (warp % kPairBX) * kPairBW + 2 * (lane % (kPairBW / 2));  // pair (px, px + 1)
+  const u32 py = ty * kTile + (warp / kPairBX) * kPairBH + lane / (kPairBW / 2);
+  const bool in0 = px < a.width && py < a.height, in1 = px + 1 < a.width && py < a.height;
+  const float2 fx = make_float2(__fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f,
+                                __fdiv_rn((float)(2 * px + 3), (float)a.width) - 1.0f);
+  const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
+  const size_t pix = (size_t)py * a.width + px;
+  float2 dpix = make_float2(1.0f, 1.0f);
+  if (DEPTH) {
+    if (in0) dpix.x = a.depth[pix];
+    if (in1) dpix.y = a.depth[pix + 1];
+  }
+  const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range)[tile];
+  const uint2 range = make_uint2(min(tr.x, a.pair_capacity), min(tr.y, a.pair_capacity));
+  const float sx = 2.0f / (float)a.width, sy = 2.0f / (float)a.height;
+  const float ox = (float)(2 * tx * kTile + 1) / (float)a.width - 1.0f;
+  const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
+  const float mx = 0.5f * sx, my = 0.5f * sy;  // 0.25 pixel
+
+  float2 T = make_float2(1.0f, 1.0f), cr = make_float2(0.0f, 0.0f), cg = cr, cb = cr, ca = cr;
+  if (!a.first) {  // the running sums of the nearer slabs
+    if (in0) {
+      const float4 c = a.state_c[pix];
+      cr.x = c.x, cg.x = c.y, cb.x = c.z, ca.x = c.w;
+      T.x = a.state_t[pix];
+    }
+    if (in1) {
+      const float4 c = a.state_c[pix + 1];
+      cr.y = c.x, cg.y = c.y, cb.y = c.z, ca.y = c.w;
+      T.y = a.state_t[pix + 1];
+    }
+  }
+  u32 frags = 0, needed = 0;
+  const float kExp = -0.5f * 1.4426950408889634f;  // -log2(e)/2
+  const float2 kExp2 = make_float2(kExp, kExp), kMinus1 = make_float2(-1.0f, -1.0f);
+  const auto stopped = [&]() {
+    return (!in0 || (!COUNT && T.x < a.t_floor)) && (!in1 || (!COUNT && T.y < a.t_floor));
+  };
+  bool done = stopped();
+  for (u32 hi = range.y; hi > range.x;) {
+    const u32 lo = (hi - range.x > (u32)kPairBatch) ? hi - kPairBatch : range.x;
+    const u32 cnt = hi - lo;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const u32 j = tid + r * kPairThreads;
+      u32 m = 0;
+      if (j < cnt) {
+        const u32 id = a.pair_splat[hi - 1 - j];  // nearest first
+        const float4* rec = a.record + 4 * (size_t)id;
+        const float4 q0 = rec[REC_CENTER], q1 = rec[REC_ROW1], q3 = rec[REC_AXES], q2 = rec[REC_COLOR];
+        s_a[j] = make_float4(-q0.x, -q0.x, -q0.y, q0.z);
+        s_b[j] = make_float4(q0.w, q1.x, q1.y, q1.z);
+        s_c[j] = make_float4(q2.x, q2.x, q2.y, q2.y);
+        s_d[j] = make_float4(q2.z, q2.z, q1.w, q1.w);
+        m = block_mask<kPairBW, kPairBH>(q0, q1, q3, ox, oy, sx, sy, mx, my);
+      }
+#pragma unroll
+      for (int b = 0; b < kPairWarps; ++b) {
+        const u32 bits = __ballot_sync(0xffffffffu, (m >> b) & 1u);
+        if (lane == 0) s_bits[b][r * kPairWarps + warp] = bits;
+      }
+    }
+    __syncthreads();
+    if (!__all_sync(0xffffffffu, done)) {
+      for (int k = 0; k < kPairWords; ++k) {
+        u32 word = s_bits[warp][k];
+        while (word) {
+          const u32 j = 32u * k + (u32)(__ffs(word) - 1);
+          word &= word - 1u;
+          const float4 A = s_a[j], B = s_b[j];
+          const float2 dx = __fadd2_rn(fx, make_float2(A.x, A.y));  // fx - cx for both pixels
+          const float dy = __fadd_rn(fy, A.z);
+          const float wu = __fmul_rn(B.x, dy), wv = __fmul_rn(B.z, dy);
+          const float u0 = __fadd_rn(__fmul_rn(A.w, dx.x), wu), u1 = __fadd_rn(__fmul_rn(A.w, dx.y), wu);
+          const float v0 = __fadd_rn(__fmul_rn(B.y, dx.x), wv), v1 = __fadd_rn(__fmul_rn(B.y, dx.y), wv);
+          bool c0 = (fabsf(u0) <= 3.0f) & (fabsf(v0) <= 3.0f);
+          bool c1 = (fabsf(u1) <= 3.0f) & (fabsf(v1) <= 3.0f);
+          if (DEPTH) {
+            c0 &= B.w < dpix.x;
+            c1 &= B.w < dpix.y;
+          }
+          if (COUNT) {
+            frags += ((c0 && in0) ? 1u : 0u) + ((c1 && in1) ? 1u : 0u);
+            needed += ((c0 && in0 && T.x >= a.t_floor) ? 1u : 0u) + ((c1 && in1 && T.y >= a.t_floor) ? 1u : 0u);
+          } else {
+            c0 &= T.x >= a.t_floor;
+            c1 &= T.y >= a.t_floor;
+          }
+          const float2 uu = make_float2(u0, u1), vv = make_float2(v0, v1);
+          const float2 e = __fmul2_rn(__ffma2_rn(uu, uu, __fmul2_rn(vv, vv)), kExp2);
+          const float2 g = make_float2(c0 ? exp2f(e.x) : 0.0f, c1 ? exp2f(e.y) : 0.0f);
+          const float4 C = s_c[j], D = s_d[j];
+          const float2 al = __fmul2_rn(make_float2(D.z, D.w), g);
+          const float2 w = __fmul2_rn(al, T);
+          cr = __ffma2_rn(w, make_float2(C.x, C.y), cr);
+          cg = __ffma2_rn(w, make_float2(C.z, C.w), cg);
+          cb = __ffma2_rn(w, make_float2(D.x, D.y), cb);
+          ca = __ffma2_rn(w, al, ca);
+          T = __ffma2_rn(w, kMinus1, T);
+        }
+        // A warp whose 64 pixels are all below t_floor stops here.
+        if (!COUNT && __all_sync(0xffffffffu, stopped())) break;
+      }
+    }
+    hi = lo;
+    done = done || stopped();
+    // Barrier before the next batch overwrites shared memory; also ends the tile once all are done.
+    if (__syncthreads_and(done)) break;
+  }
+  const bool finished = __syncthreads_and(done);
+  if (finished && !a.last && tid == 0) atomicOr(a.tile_done + (tile >> 5), 1u << (tile & 31u));
+  if (COUNT) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      frags += __shfl_xor_sync(0xffffffffu, frags, o);
+      needed += __shfl_xor_sync(0xffffffffu, needed, o);
+    }
+    if (lane == 0 && frags) atomicAdd(a.fragments, (unsigned long long)frags);
+    if (lane == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
+  }
+  if (!finished && !a.last) {  // a farther slab continues these pixels
+    if (in0) {
+      a.state_c[pix] = make_float4(cr.x, cg.x, cb.x, ca.x);
+      a.state_t[pix] = T.x;
+    }
+    if (in1) {
+      a.state_c[pix + 1] = make_float4(cr.y, cg.y, cb.y, ca.y);
+      a.state_t[pix + 1] = T.y;
+    }
+    return;
+  }
+  const auto q = [](float x) { return (unsigned char)__float2uint_rn(__saturatef(x) * 255.0f); };
+  if (in0) {
+    const float alpha = ca.x + T.x;
+    if (a.out_rgba) reinterpret_cast<float4*>(a.out_rgba)[pix] = make_float4(cr.x, cg.x, cb.x, alpha);
+    if (a.out_bgra) a.out_bgra[pix] = make_uchar4(q(cb.x), q(cg.x), q(cr.x), q(alpha));
+  }
+  if (in1) {
+    const float alpha = ca.y + T.y;
+    if (a.out_rgba) reinterpret_cast<float4*>(a.out_rgba)[pix + 1] = make_float4(cr.y, cg.y, cb.y, alpha);
+    if (a.out_bgra) a.out_bgra[pix + 1] = make_uchar4(q(cb.y), q(cg.y), q(cr.y), q(alpha));
+  }
+}
+
 cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
   const u32 tiles = a.tiles_x * a.tiles_y;
   if (tiles == 0) return cudaSuccess;
   const bool depth = a.depth != nullptr, count = a.fragments != nullptr;
+  const bool pairs = a.lean && !a.nproc;  // frames beside other frames: fewer instructions per pixel
   if (a.nproc)
     k_raster<false, false, true><<<tiles, kRasterThreads, 0, stream>>>(a);
+  else if (pairs && depth && count)
+    k_raster_pairs<true, true><<<tiles, kPairThreads, 0, stream>>>(a);
+  else if (pairs && depth)
+    k_raster_pairs<true, false><<<tiles, kPairThreads, 0, stream>>>(a);
+  else if (pairs && count)
+    k_raster_pairs<false, true><<<tiles, kPairThreads, 0, stream>>>(a);
+  else if (pairs)
+    k_raster_pairs<false, false><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (depth && count)
     k_raster<true, true, false><<<tiles, kRasterThreads, 0, stream>>>(a);
   else if (depth)
