@@ -198,12 +198,13 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
 constexpr int kPairThreads = kTile * kTile / 2;
 constexpr int kPairWarps = kPairThreads / 32;  // 4 blocks of 64 pixels
 constexpr int kPairBatch = 256;                // records per batch, two per thread
+constexpr int kPairLoads = kPairBatch / kPairThreads;
 constexpr int kPairWords = kPairBatch / 32;
 
 constexpr int kPairBW = 8, kPairBH = 8, kPairBX = kTile / kPairBW;  // 8x8 blocks, 2 x 2 per tile
 static_assert(kPairWarps * kPairBW * kPairBH == kTile * kTile && kPairBW * kPairBH == 64, "pair blocks");
 
-template <bool DEPTH, bool COUNT>
+template <bool DEPTH, bool COUNT, bool TRAIN>
 __global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterArgs a) {
   __shared__ float4 s_a[kPairBatch];  // (-cx, -cx, -cy, m00)
   __shared__ float4 s_b[kPairBatch];  // (m01, m10, m11, z)
@@ -246,7 +247,7 @@ __global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterAr
       T.y = a.state_t[pix + 1];
     }
   }
-  u32 frags = 0, needed = 0;
+  u32 frags = 0, needed = 0, blended0 = 0, blended1 = 0;
   const float kExp = -0.5f * 1.4426950408889634f;  // -log2(e)/2
   const float2 kExp2 = make_float2(kExp, kExp), kMinus1 = make_float2(-1.0f, -1.0f);
   const auto stopped = [&]() {
@@ -257,7 +258,7 @@ __global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterAr
     const u32 lo = (hi - range.x > (u32)kPairBatch) ? hi - kPairBatch : range.x;
     const u32 cnt = hi - lo;
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < kPairLoads; ++r) {
       const u32 j = tid + r * kPairThreads;
       u32 m = 0;
       if (j < cnt) {
@@ -302,6 +303,10 @@ __global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterAr
             c0 &= T.x >= a.t_floor;
             c1 &= T.y >= a.t_floor;
           }
+          if (TRAIN) {  // processing index + 1 (0 = nearest)
+            if (c0) blended0 = range.y - hi + j + 1;
+            if (c1) blended1 = range.y - hi + j + 1;
+          }
           const float2 uu = make_float2(u0, u1), vv = make_float2(v0, v1);
           const float2 e = __fmul2_rn(__ffma2_rn(uu, uu, __fmul2_rn(vv, vv)), kExp2);
           const float2 g = make_float2(c0 ? exp2f(e.x) : 0.0f, c1 ? exp2f(e.y) : 0.0f);
@@ -334,6 +339,16 @@ __global__ __launch_bounds__(kPairThreads, 8) void k_raster_pairs(const RasterAr
     if (lane == 0 && frags) atomicAdd(a.fragments, (unsigned long long)frags);
     if (lane == 0 && needed) atomicAdd(a.fragments + 1, (unsigned long long)needed);
   }
+  if (TRAIN) {
+    if (in0) {
+      a.nproc[pix] = blended0;
+      a.state_t[pix] = T.x;
+    }
+    if (in1) {
+      a.nproc[pix + 1] = blended1;
+      a.state_t[pix + 1] = T.y;
+    }
+  }
   if (!finished && !a.last) {  // a farther slab continues these pixels
     if (in0) {
       a.state_c[pix] = make_float4(cr.x, cg.x, cb.x, ca.x);
@@ -362,17 +377,19 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
   const u32 tiles = a.tiles_x * a.tiles_y;
   if (tiles == 0) return cudaSuccess;
   const bool depth = a.depth != nullptr, count = a.fragments != nullptr;
-  const bool pairs = a.lean && !a.nproc;  // frames beside other frames: fewer instructions per pixel
-  if (a.nproc)
+  const bool pairs = a.lean;  // frames beside other frames: fewer instructions per pixel
+  if (a.nproc && pairs)
+    k_raster_pairs<false, false, true><<<tiles, kPairThreads, 0, stream>>>(a);
+  else if (a.nproc)
     k_raster<false, false, true><<<tiles, kRasterThreads, 0, stream>>>(a);
   else if (pairs && depth && count)
-    k_raster_pairs<true, true><<<tiles, kPairThreads, 0, stream>>>(a);
+    k_raster_pairs<true, true, false><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (pairs && depth)
-    k_raster_pairs<true, false><<<tiles, kPairThreads, 0, stream>>>(a);
+    k_raster_pairs<true, false, false><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (pairs && count)
-    k_raster_pairs<false, true><<<tiles, kPairThreads, 0, stream>>>(a);
+    k_raster_pairs<false, true, false><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (pairs)
-    k_raster_pairs<false, false><<<tiles, kPairThreads, 0, stream>>>(a);
+    k_raster_pairs<false, false, false><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (depth && count)
     k_raster<true, true, false><<<tiles, kRasterThreads, 0, stream>>>(a);
   else if (depth)
