@@ -439,106 +439,131 @@ __device__ __forceinline__ float warp_sum9(float v[9], float* v8) {
   return t;
 }
 
-constexpr u32 kDirectLanes = 8;  // a record covering at most this many pixels of a warp skips the reduction
+constexpr u32 kDirectLanes = 8;  // a record that at most this many lanes of a warp take skips the reduction
 
-// Each warp (an 8x4 pixel block) walks only the records that can touch its block, reduces the 9
-// per-splat values over its 32 pixels (warp_sum9) and adds them with one atomic per value; a record
-// that covers only a few of the warp's pixels is added by those lanes directly.
-__global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const RasterBackwardArgs a) {
-  __shared__ float4 s_q0[kRasterThreads];
-  __shared__ float4 s_q1[kRasterThreads];
-  __shared__ float4 s_q2[kRasterThreads];
-  __shared__ u32 s_id[kRasterThreads];
-  __shared__ u32 s_bits[kWarps][kWarps];
+// Two horizontally adjacent pixels per thread and 8x8 warp blocks, as in k_raster_pairs: each warp walks
+// only the records that can touch its block, a thread adds its two pixels' 9 values before the warp
+// reduction (warp_sum9), so one reduction serves 64 pixels, and the per-pixel chain runs as packed FP32
+// pairs; a record that few lanes take is added by those lanes directly.  A pixel that does not take a
+// record gets G = 0, which leaves its T and S unchanged and adds zeros.
+__global__ __launch_bounds__(kPairThreads, 8) void k_raster_backward(const RasterBackwardArgs a) {
+  __shared__ float4 s_a[kPairBatch];  // (-cx, -cx, -cy, m00)
+  __shared__ float4 s_b[kPairBatch];  // (m01, m10, m11, -)
+  __shared__ float4 s_c[kPairBatch];  // (r, r, g, g)
+  __shared__ float4 s_d[kPairBatch];  // (b, b, opacity, opacity)
+  __shared__ u32 s_id[kPairBatch];
+  __shared__ u32 s_bits[kPairWarps][kPairWords];
   __shared__ u32 s_nmax;
   const u32 tile = blockIdx.x;
   const u32 tx = tile % a.tiles_x, ty = tile / a.tiles_x;
   const u32 tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const u32 px = tx * kTile + (warp % kBlocksX) * kBlockW + lane % kBlockW;
-  const u32 py = ty * kTile + (warp / kBlocksX) * kBlockH + lane / kBlockW;
-  const bool inside = px < a.width && py < a.height;
+  const u32 px = tx * kTile + (warp % kPairBX) * kPairBW + 2 * (lane % (kPairBW / 2));  // pair (px, px + 1)
+  const u32 py = ty * kTile + (warp / kPairBX) * kPairBH + lane / (kPairBW / 2);
+  const bool in0 = px < a.width && py < a.height, in1 = px + 1 < a.width && py < a.height;
   const size_t pix = (size_t)py * a.width + px;
-  const float fx = __fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f;
+  const float2 fx = make_float2(__fdiv_rn((float)(2 * px + 1), (float)a.width) - 1.0f,
+                                __fdiv_rn((float)(2 * px + 3), (float)a.width) - 1.0f);
   const float fy = __fdiv_rn((float)(2 * py + 1), (float)a.height) - 1.0f;
-  float Tcur = inside ? a.state_t[pix] : 1.0f;
-  const float4 g = inside ? a.grad_rgba[pix] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  float S = Tcur * g.w;
+  float2 Tcur = make_float2(in0 ? a.state_t[pix] : 1.0f, in1 ? a.state_t[pix + 1] : 1.0f);
+  const float4 g0 = in0 ? a.grad_rgba[pix] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 g1 = in1 ? a.grad_rgba[pix + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float2 gx = make_float2(g0.x, g1.x), gy = make_float2(g0.y, g1.y), gz = make_float2(g0.z, g1.z);
+  const float2 gw = make_float2(g0.w, g1.w), gw2 = make_float2(2.0f * g0.w, 2.0f * g1.w);
+  float2 S = __fmul2_rn(Tcur, gw);
   const float sx = 2.0f / (float)a.width, sy = 2.0f / (float)a.height;
   const float ox = (float)(2 * tx * kTile + 1) / (float)a.width - 1.0f;
   const float oy = (float)(2 * ty * kTile + 1) / (float)a.height - 1.0f;
   const float mx = 0.5f * sx, my = 0.5f * sy;
   const float kExp = -0.5f * 1.4426950408889634f;
+  const float2 kExp2 = make_float2(kExp, kExp), kMinus1 = make_float2(-1.0f, -1.0f);
   for (int slab = (int)a.slabs - 1; slab >= 0; --slab) {  // farthest slab first: the reverse of the forward
-    const u32 n = inside ? a.nproc[(size_t)slab * a.nproc_stride + pix] : 0u;
-    u32 wmax = n;  // the most list entries any pixel of this warp blended
+    const u32 n0 = in0 ? a.nproc[(size_t)slab * a.nproc_stride + pix] : 0u;
+    const u32 n1 = in1 ? a.nproc[(size_t)slab * a.nproc_stride + pix + 1] : 0u;
+    u32 wmax = max(n0, n1);  // the most list entries any pixel of this warp blended
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
     if (tid == 0) s_nmax = 0;
     __syncthreads();
-    if (n) atomicMax(&s_nmax, n);
+    if (lane == 0 && wmax) atomicMax(&s_nmax, wmax);
     __syncthreads();
     const uint2 tr = reinterpret_cast<const uint2*>(a.tile_range + (size_t)slab * a.range_stride)[tile];
     const u32 hi = min(tr.y, a.pair_capacity);
     const u32 first = hi - min(s_nmax, hi - min(tr.x, a.pair_capacity));  // farthest entry any pixel blended
-    for (u32 lo = first; lo < hi; lo += kRasterThreads) {  // farthest first: the reverse of the forward
-      const u32 cnt = min((u32)kRasterThreads, hi - lo);
-      u32 mask = 0;
-      if (tid < cnt) {
-        const u32 id = a.pair_splat[lo + tid];
-        const float4* rec = a.record + 4 * (size_t)id;
-        const float4 q0 = rec[REC_CENTER], q1 = rec[REC_ROW1], q3 = rec[REC_AXES];
-        s_q0[tid] = q0;
-        s_q1[tid] = q1;
-        s_q2[tid] = rec[REC_COLOR];
-        s_id[tid] = id;
-        mask = block_mask(q0, q1, q3, ox, oy, sx, sy, mx, my);
-      }
+    for (u32 lo = first; lo < hi; lo += kPairBatch) {  // farthest first: the reverse of the forward
+      const u32 cnt = min((u32)kPairBatch, hi - lo);
 #pragma unroll
-      for (int b = 0; b < kWarps; ++b) {
-        const u32 bits = __ballot_sync(0xffffffffu, (mask >> b) & 1u);
-        if (lane == 0) s_bits[b][warp] = bits;
+      for (int r = 0; r < kPairLoads; ++r) {
+        const u32 j = tid + r * kPairThreads;
+        u32 m = 0;
+        if (j < cnt) {
+          const u32 id = a.pair_splat[lo + j];
+          const float4* rec = a.record + 4 * (size_t)id;
+          const float4 q0 = rec[REC_CENTER], q1 = rec[REC_ROW1], q3 = rec[REC_AXES], q2 = rec[REC_COLOR];
+          s_a[j] = make_float4(-q0.x, -q0.x, -q0.y, q0.z);
+          s_b[j] = make_float4(q0.w, q1.x, q1.y, 0.0f);
+          s_c[j] = make_float4(q2.x, q2.x, q2.y, q2.y);
+          s_d[j] = make_float4(q2.z, q2.z, q1.w, q1.w);
+          s_id[j] = id;
+          m = block_mask<kPairBW, kPairBH>(q0, q1, q3, ox, oy, sx, sy, mx, my);
+        }
+#pragma unroll
+        for (int b = 0; b < kPairWarps; ++b) {
+          const u32 bits = __ballot_sync(0xffffffffu, (m >> b) & 1u);
+          if (lane == 0) s_bits[b][r * kPairWarps + warp] = bits;
+        }
       }
       __syncthreads();
-      for (int k = 0; k < kWarps; ++k) {
+      for (int k = 0; k < kPairWords; ++k) {
         u32 word = s_bits[warp][k];
         while (word) {
           const u32 j = 32u * k + (u32)(__ffs(word) - 1);
           word &= word - 1u;
           const u32 kproc = hi - 1 - (lo + j);  // processing index in the forward (0 = nearest)
           if (kproc >= wmax) continue;           // behind every pixel of this warp (warp-uniform)
-          const float4 q0 = s_q0[j], q1 = s_q1[j];
-          const float dx = __fsub_rn(fx, q0.x), dy = __fsub_rn(fy, q0.y);
-          const float u = __fadd_rn(__fmul_rn(q0.z, dx), __fmul_rn(q0.w, dy));
-          const float v = __fadd_rn(__fmul_rn(q1.x, dx), __fmul_rn(q1.y, dy));
-          const bool on = kproc < n && (fabsf(u) <= 3.0f) & (fabsf(v) <= 3.0f);
+          const float4 A = s_a[j], B = s_b[j];
+          const float2 dx = __fadd2_rn(fx, make_float2(A.x, A.y));
+          const float dy = __fadd_rn(fy, A.z);
+          const float wu = __fmul_rn(B.x, dy), wv = __fmul_rn(B.z, dy);
+          const float u0 = __fadd_rn(__fmul_rn(A.w, dx.x), wu), u1 = __fadd_rn(__fmul_rn(A.w, dx.y), wu);
+          const float v0 = __fadd_rn(__fmul_rn(B.y, dx.x), wv), v1 = __fadd_rn(__fmul_rn(B.y, dx.y), wv);
+          const bool on0 = kproc < n0 && (fabsf(u0) <= 3.0f) & (fabsf(v0) <= 3.0f);
+          const bool on1 = kproc < n1 && (fabsf(u1) <= 3.0f) & (fabsf(v1) <= 3.0f);
+          const bool on = on0 || on1;
           float r[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
           if (on) {
-            const float4 q2 = s_q2[j];
-            const float G = exp2f(kExp * (u * u + v * v));
-            const float al = q1.w * G;
-            const float inv = __fdividef(1.0f, fmaxf(1.0f - al, 1e-6f));
-            const float Ti = Tcur * inv;
-            const float cg = q2.x * g.x + q2.y * g.y + q2.z * g.z;
-            const float dLda = Ti * (cg + 2.0f * al * g.w) - S * inv;
-            S += (al * cg + al * al * g.w) * Ti;
+            const float2 uu = make_float2(u0, u1), vv = make_float2(v0, v1);
+            const float2 e = __fmul2_rn(__ffma2_rn(uu, uu, __fmul2_rn(vv, vv)), kExp2);
+            const float2 G = make_float2(on0 ? exp2f(e.x) : 0.0f, on1 ? exp2f(e.y) : 0.0f);
+            const float4 C = s_c[j], D = s_d[j];
+            const float2 al = __fmul2_rn(make_float2(D.z, D.w), G);
+            const float2 inv = make_float2(__fdividef(1.0f, fmaxf(1.0f - al.x, 1e-6f)),
+                                           __fdividef(1.0f, fmaxf(1.0f - al.y, 1e-6f)));
+            const float2 Ti = __fmul2_rn(Tcur, inv);
+            const float2 cg = __ffma2_rn(make_float2(C.x, C.y), gx,
+                                         __ffma2_rn(make_float2(C.z, C.w), gy, __fmul2_rn(make_float2(D.x, D.y), gz)));
+            const float2 dLda = __ffma2_rn(__fmul2_rn(S, inv), kMinus1, __fmul2_rn(Ti, __ffma2_rn(al, gw2, cg)));
+            S = __ffma2_rn(__fmul2_rn(al, __ffma2_rn(al, gw, cg)), Ti, S);
             Tcur = Ti;
-            const float P = dLda * G;  // dL/do of this pixel; dL/dq = -o P / 2
-            const float pdx = P * dx, pdy = P * dy;
-            r[0] = P;
-            r[1] = pdx;
-            r[2] = pdy;
-            r[3] = pdx * dx;
-            r[4] = pdy * dy;
-            r[5] = pdx * dy;
-            const float w = al * Ti;
-            r[6] = w * g.x;
-            r[7] = w * g.y;
-            r[8] = w * g.z;
+            const float2 P = __fmul2_rn(dLda, G);  // dL/do of each pixel; dL/dq = -o P / 2
+            const float2 dy2 = make_float2(dy, dy);
+            const float2 pdx = __fmul2_rn(P, dx), pdy = __fmul2_rn(P, dy2);
+            const float2 pxx = __fmul2_rn(pdx, dx), pyy = __fmul2_rn(pdy, dy2), pxy = __fmul2_rn(pdx, dy2);
+            const float2 w = __fmul2_rn(al, Ti);
+            const float2 wr = __fmul2_rn(w, gx), wg = __fmul2_rn(w, gy), wb = __fmul2_rn(w, gz);
+            r[0] = P.x + P.y;
+            r[1] = pdx.x + pdx.y;
+            r[2] = pdy.x + pdy.y;
+            r[3] = pxx.x + pxx.y;
+            r[4] = pyy.x + pyy.y;
+            r[5] = pxy.x + pxy.y;
+            r[6] = wr.x + wr.y;
+            r[7] = wg.x + wg.y;
+            r[8] = wb.x + wb.y;
           }
           const u32 onmask = __ballot_sync(0xffffffffu, on);
           if (onmask) {
             float* dst = a.grad_rec + (size_t)s_id[j] * kGradRec;
-            if (__popc(onmask) <= kDirectLanes) {  // few pixels: their own atomics beat a warp reduction
+            if (__popc(onmask) <= kDirectLanes) {  // few lanes: their own atomics beat a warp reduction
               if (on) {
 #pragma unroll
                 for (int q = 0; q < 9; ++q) atomicAdd(dst + q, r[q]);
@@ -563,7 +588,7 @@ __global__ __launch_bounds__(kRasterThreads) void k_raster_backward(const Raster
 cudaError_t launch_raster_backward(const RasterBackwardArgs& a, cudaStream_t stream) {
   const u32 tiles = a.tiles_x * a.tiles_y;
   if (tiles == 0) return cudaSuccess;
-  k_raster_backward<<<tiles, kRasterThreads, 0, stream>>>(a);
+  k_raster_backward<<<tiles, kPairThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
