@@ -866,14 +866,15 @@ def run_ours(args):
                 "form": f"gs_viewer_submit per step ({FRAMES_IN_FLIGHT} frames in flight) + the RGBA image of "
                         "each frame copied to pinned host memory; a copy overlaps the following frames"},
         "gpu_launches": None,
-        "roofline": {"bound": "fp32", "kernel": "k_raster", "achieved": achieved, "peak": fp32_peak,
+        "roofline": {"bound": "fp32", "kernel": "k_raster_pairs (nearest slab) + k_raster (farther slab)",
+                     "achieved": achieved, "peak": fp32_peak,
                      "unit": "T lane-ops/s", "frac": achieved / fp32_peak,
                      "traffic": raster_profile().get("dram_bytes_per_launch"),
                      "issue_active_ncu": raster_profile().get("issue_active"),
                      "peak_source": f"nominal {sms} SMs x 128 FP32 lanes x {sm_max:.0f} MHz (max SM clock)",
                      "work": f"{OPS_PER_FRAGMENT} FP32 lane-ops per covered (pixel, splat) pair met front to "
                              "back while the pixel's transmittance is >= the transmittance floor (1e-4)",
-                     "lean_form": {"kernel": "k_raster_pairs", "ms": float(lean_stage[:, 5].mean()),
+                     "lean_form": {"kernel": "k_raster_pairs (every slab)", "ms": float(lean_stage[:, 5].mean()),
                                    "achieved": achieved_lean, "frac": achieved_lean / fp32_peak,
                                    "form": "the raster of the headline's viewer slots (two pixels per thread, "
                                            "packed FP32 blend), timed alone on the direct path"}},

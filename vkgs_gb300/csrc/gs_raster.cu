@@ -377,7 +377,11 @@ cudaError_t launch_raster(const RasterArgs& a, cudaStream_t stream) {
   const u32 tiles = a.tiles_x * a.tiles_y;
   if (tiles == 0) return cudaSuccess;
   const bool depth = a.depth != nullptr, count = a.fragments != nullptr;
-  const bool pairs = a.lean;  // frames beside other frames: fewer instructions per pixel
+  // Two pixels per thread issue fewer instructions per pixel but keep a 64-pixel warp walking until its
+  // last pixel stops: they serve frames that run beside other frames (issue-bound) and the nearest
+  // slab, where pixels start at full transmittance; a farther slab, whose pixels are mostly near the
+  // floor already, takes one pixel per thread when the frame has the GPU to itself.
+  const bool pairs = a.lean || a.first;
   if (a.nproc && pairs)
     k_raster_pairs<false, false, true><<<tiles, kPairThreads, 0, stream>>>(a);
   else if (a.nproc)
