@@ -33,8 +33,8 @@ UNITS = {
     "gs_bin.cu": ["--fmad=false"],
     "gs_raster.cu": ["-ftz=true"],
     "gs_noalloc.cu": [],
-    # the activation must reproduce gs_ply.cu's bits (shared device code, same flags)
-    "gs_train.cu": ["--fmad=false"],
+    # the projection backward: gradients, no bit-exactness requirement (FMA contraction on)
+    "gs_train.cu": [],
 }
 HEADERS = ["gs_common.cuh", "gs_internal.h"]
 

@@ -1,4 +1,5 @@
-// gs_ply.cu -- parse_ply.comp: activation of raw 3DGS PLY rows into the splat buffers.
+// gs_ply.cu -- parse_ply.comp: activation of raw 3DGS PLY rows into the splat buffers, and the same
+// activation of the differentiable path's raw parameters (k_activate).
 //
 // Follows src/shader/parse_ply.comp:43-97 with the row layout of splat_load_thread.cc:114-135
 // (offsets[0..58] are float offsets inside a row, offsets[59] the row stride).  Compiled with
@@ -34,6 +35,27 @@ cudaError_t launch_parse_ply(const float* rows, u32 count, const PlyOffsets& off
                              float* opacity, uint16_t* sh, cudaStream_t stream) {
   if (count == 0) return cudaSuccess;
   k_parse_ply<<<(count + 255) / 256, 256, 0, stream>>>(rows, count, off, position, cov3d, opacity, sh);
+  return cudaGetLastError();
+}
+
+// parse_ply.comp's activation of the raw parameters (the same device code as k_parse_ply, so the records
+// of the differentiable forward are the plain path's for the same splats); SH stay FP32.
+__global__ void k_activate(const TrainArgs a) {
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
+    const float4 q = reinterpret_cast<const float4*>(a.quats)[id];
+    activate_cov3d(a.log_scales[3 * id], a.log_scales[3 * id + 1], a.log_scales[3 * id + 2], q.x, q.y, q.z, q.w,
+                   a.cov3d + 6 * (size_t)id);
+    a.opacity[id] = activate_opacity(a.opacity_logits[id]);
+    a.position[3 * id] = a.means[3 * id];
+    a.position[3 * id + 1] = a.means[3 * id + 1];
+    a.position[3 * id + 2] = a.means[3 * id + 2];
+  }
+}
+
+cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream) {
+  if (a.n == 0) return cudaSuccess;
+  k_activate<<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -1,5 +1,6 @@
-// gs_train.cu -- the differentiable path's per-splat kernels: activation (forward) and the projection
-// backward.  The blend backward is in gs_raster.cu.
+// gs_train.cu -- the differentiable path's projection backward (the activation of its forward is in
+// gs_ply.cu, beside the loader's; the blend backward is in gs_raster.cu).  Gradients carry no
+// bit-exactness requirement, so this unit is compiled with FMA contraction.
 //
 // Forward chain (the reference's formulas, as in gs_ply.cu / gs_cull.cu):
 //   parse_ply.comp:62-88   s = exp(log_s), q = quat/|quat| (x, y, z, w), R(q), cov3d = R diag(s^2) R^T,
@@ -22,27 +23,6 @@ __device__ __forceinline__ void quat_rotation(float x, float y, float z, float w
   R[0][0] = 1.0f - 2.0f * (yy + zz), R[0][1] = 2.0f * (xy - wz), R[0][2] = 2.0f * (xz + wy);
   R[1][0] = 2.0f * (xy + wz), R[1][1] = 1.0f - 2.0f * (xx + zz), R[1][2] = 2.0f * (yz - wx);
   R[2][0] = 2.0f * (xz - wy), R[2][1] = 2.0f * (yz + wx), R[2][2] = 1.0f - 2.0f * (xx + yy);
-}
-
-// parse_ply.comp's activation of the raw parameters (the same device code as k_parse_ply, so the records
-// of the differentiable forward are the plain path's for the same splats); SH stay FP32.
-__global__ void k_activate(const TrainArgs a) {
-  const u32 stride = gridDim.x * blockDim.x;
-  for (u32 id = blockIdx.x * blockDim.x + threadIdx.x; id < a.n; id += stride) {
-    const float4 q = reinterpret_cast<const float4*>(a.quats)[id];
-    activate_cov3d(a.log_scales[3 * id], a.log_scales[3 * id + 1], a.log_scales[3 * id + 2], q.x, q.y, q.z, q.w,
-                   a.cov3d + 6 * (size_t)id);
-    a.opacity[id] = activate_opacity(a.opacity_logits[id]);
-    a.position[3 * id] = a.means[3 * id];
-    a.position[3 * id + 1] = a.means[3 * id + 1];
-    a.position[3 * id + 2] = a.means[3 * id + 2];
-  }
-}
-
-cudaError_t launch_activate(const TrainArgs& a, cudaStream_t stream) {
-  if (a.n == 0) return cudaSuccess;
-  k_activate<<<min((a.n + 255) / 256, 65535u), 256, 0, stream>>>(a);
-  return cudaGetLastError();
 }
 
 // Degree-3 SH basis B_k(d), the reference's coefficient order (projection.comp:140-163).
