@@ -65,6 +65,8 @@ def test_null_arguments_are_rejected_without_a_device(lib):
     assert lib.gs_context_set_transmittance_floor(None, 1e-4) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_context_set_batch_lanes(None, 0) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_context_set_batch_shared_cull(None, 1) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_cull_staging(None, 1) == L.GS_ERROR_INVALID_ARGUMENT
+    assert lib.gs_context_set_lean(None, 1) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_context_set_train_slab_min(None, 0) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_render_batched(None, None, 0, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
     assert lib.gs_train_forward(None, None, None, None, None) == L.GS_ERROR_INVALID_ARGUMENT
