@@ -887,7 +887,8 @@ gs_status gs_train_backward(gs_context* c, const gs_train_params* p, const gs_ca
 }
 
 // Batched differentiable path: view v is drawn by render lane v, which keeps that view's forward state
-// for the backward; the lanes' projection backwards add into the shared gradients atomically.
+// for the backward; the lanes' blend backwards run concurrently, then one projection backward adds the
+// gradients of all views into the caller's buffers.
 static gs_status fork_lanes(gs_context* c, u32 used, cudaStream_t st) {
   if (cudaEventRecord(c->batch_fork, st) != cudaSuccess) return GS_ERROR_CUDA;
   for (u32 l = 0; l < used; ++l)

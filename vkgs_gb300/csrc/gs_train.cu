@@ -78,20 +78,34 @@ __device__ __forceinline__ float mel(const float* m, int r, int c) { return m[c 
 
 constexpr u32 kPbThreads = 128;
 
+// Scale s = exp(log_s), the normalised quaternion, its length and R(q) of splat id (parse_ply.comp:62-88).
+__device__ __forceinline__ void scale_rotation(const TrainArgs& a, u32 id, float sc[3], float qn[4], float& qlen,
+                                               float R[3][3]) {
+  sc[0] = expf(a.log_scales[3 * id]), sc[1] = expf(a.log_scales[3 * id + 1]), sc[2] = expf(a.log_scales[3 * id + 2]);
+  const float4 q4 = reinterpret_cast<const float4*>(a.quats)[id];
+  qlen = sqrtf(((q4.x * q4.x + q4.y * q4.y) + q4.z * q4.z) + q4.w * q4.w);
+  qn[0] = q4.x / qlen, qn[1] = q4.y / qlen, qn[2] = q4.z / qlen, qn[3] = q4.w / qlen;
+  quat_rotation(qn[0], qn[1], qn[2], qn[3], R);
+}
+
 // Projection backward over every view of one step: a thread per splat walks the views whose blend
 // backward reached the splat and accumulates the raw-parameter gradients in registers (SH in shared
 // memory), then adds them to the caller's buffers once -- the splat's parameters are read once and no
 // atomics are needed however many views there are.  The final maps (quaternion normalisation, exp of
 // the log-scales, sigmoid of the logit) are linear in the accumulated gradients, so they are applied
 // after the sum over views.
-__global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainViews vs, const TrainArgs a) {
+// 4 CTAs per SM: 128 registers, no spills (168 without the bound, 3 CTAs per SM)
+__global__ __launch_bounds__(kPbThreads, 4) void k_project_backward(const TrainViews vs, const TrainArgs a) {
   __shared__ float s_gsh[48][kPbThreads];
   const u32 tid = threadIdx.x;
   const u32 stride = gridDim.x * blockDim.x;
   for (u32 id = blockIdx.x * blockDim.x + tid; id < a.n; id += stride) {
     bool ready = false;  // forward quantities of the splat computed (on the first view that needs them)
-    float sc[3], qn[4], qlen = 1.0f, R[3][3], Sg[3][3], o = 0.0f, pos[3];
-    float gpos[3] = {0.0f, 0.0f, 0.0f}, gsc[3] = {0.0f, 0.0f, 0.0f}, gq[4] = {0.0f, 0.0f, 0.0f, 0.0f}, g_o = 0.0f;
+    float Sg[3][3], o = 0.0f, pos[3];
+    // dL/dcov3d summed over the views: cov3d does not depend on the view, so its chain back to scale and
+    // rotation runs once per splat, after the view loop
+    float gSum[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+    float gpos[3] = {0.0f, 0.0f, 0.0f}, g_o = 0.0f;
     const float4* __restrict__ shp = reinterpret_cast<const float4*>(a.sh + 48 * (size_t)id);
 #pragma unroll 1
     for (u32 v = 0; v < vs.count; ++v) {
@@ -109,12 +123,8 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
       if (!ready) {        // ---- activation (parse_ply.comp:62-88)
         ready = true;
         for (int k = 0; k < 48; ++k) s_gsh[k][tid] = 0.0f;
-        const float ls0 = a.log_scales[3 * id], ls1 = a.log_scales[3 * id + 1], ls2 = a.log_scales[3 * id + 2];
-        sc[0] = expf(ls0), sc[1] = expf(ls1), sc[2] = expf(ls2);
-        const float4 q4 = reinterpret_cast<const float4*>(a.quats)[id];
-        qlen = sqrtf(((q4.x * q4.x + q4.y * q4.y) + q4.z * q4.z) + q4.w * q4.w);
-        qn[0] = q4.x / qlen, qn[1] = q4.y / qlen, qn[2] = q4.z / qlen, qn[3] = q4.w / qlen;
-        quat_rotation(qn[0], qn[1], qn[2], qn[3], R);
+        float sc[3], qn[4], qlen, R[3][3];
+        scale_rotation(a, id, sc, qn, qlen, R);
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -271,28 +281,37 @@ __global__ __launch_bounds__(kPbThreads) void k_project_backward(const TrainView
 #pragma unroll
         for (int c = 0; c < 3; ++c) gS[r][c] = tA[r][0] * A(0, c) + tA[r][1] * A(1, c) + tA[r][2] * A(2, c);
 
-      // ---- cov3d = (R S)(R S)^T -> scale, rotation -> (unnormalised) quaternion gradient
-      float gR[3][3];
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          // d cov / d M_ri with M = R diag(s): (gS + gS^T) M
-          const float gM = (gS[r][0] + gS[0][r]) * R[0][i] * sc[i] + (gS[r][1] + gS[1][r]) * R[1][i] * sc[i] +
-                           (gS[r][2] + gS[2][r]) * R[2][i] * sc[i];
-          gsc[i] += gM * R[r][i];
-          gR[r][i] = gM * sc[i];
-        }
-      const float qx = qn[0], qy = qn[1], qz = qn[2], qw = qn[3];
-      gq[0] += 2.0f * (qy * (gR[0][1] + gR[1][0]) + qz * (gR[0][2] + gR[2][0]) + qw * (gR[2][1] - gR[1][2])) -
-               4.0f * qx * (gR[1][1] + gR[2][2]);
-      gq[1] += 2.0f * (qx * (gR[0][1] + gR[1][0]) + qw * (gR[0][2] - gR[2][0]) + qz * (gR[1][2] + gR[2][1])) -
-               4.0f * qy * (gR[0][0] + gR[2][2]);
-      gq[2] += 2.0f * (qw * (gR[1][0] - gR[0][1]) + qx * (gR[0][2] + gR[2][0]) + qy * (gR[1][2] + gR[2][1])) -
-               4.0f * qz * (gR[0][0] + gR[1][1]);
-      gq[3] += 2.0f * (qz * (gR[1][0] - gR[0][1]) + qy * (gR[0][2] - gR[2][0]) + qx * (gR[2][1] - gR[1][2]));
+        for (int c = 0; c < 3; ++c) gSum[r][c] += gS[r][c];
     }
     if (!ready) continue;
+    // ---- cov3d = (R S)(R S)^T -> scale, rotation -> (unnormalised) quaternion gradient, once for the sum
+    // over the views (recomputed here rather than kept live through the view loop)
+    float sc[3], qn[4], qlen, R[3][3];
+    scale_rotation(a, id, sc, qn, qlen, R);
+    float gR[3][3], gsc[3] = {0.0f, 0.0f, 0.0f}, gq[4];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        // d cov / d M_ri with M = R diag(s): (gS + gS^T) M
+        const float gM = (gSum[r][0] + gSum[0][r]) * R[0][i] * sc[i] + (gSum[r][1] + gSum[1][r]) * R[1][i] * sc[i] +
+                         (gSum[r][2] + gSum[2][r]) * R[2][i] * sc[i];
+        gsc[i] += gM * R[r][i];
+        gR[r][i] = gM * sc[i];
+      }
+    {
+      const float qx = qn[0], qy = qn[1], qz = qn[2], qw = qn[3];
+      gq[0] = 2.0f * (qy * (gR[0][1] + gR[1][0]) + qz * (gR[0][2] + gR[2][0]) + qw * (gR[2][1] - gR[1][2])) -
+              4.0f * qx * (gR[1][1] + gR[2][2]);
+      gq[1] = 2.0f * (qx * (gR[0][1] + gR[1][0]) + qw * (gR[0][2] - gR[2][0]) + qz * (gR[1][2] + gR[2][1])) -
+              4.0f * qy * (gR[0][0] + gR[2][2]);
+      gq[2] = 2.0f * (qw * (gR[1][0] - gR[0][1]) + qx * (gR[0][2] + gR[2][0]) + qy * (gR[1][2] + gR[2][1])) -
+              4.0f * qz * (gR[0][0] + gR[1][1]);
+      gq[3] = 2.0f * (qz * (gR[1][0] - gR[0][1]) + qy * (gR[0][2] - gR[2][0]) + qx * (gR[2][1] - gR[1][2]));
+    }
     // ---- the linear maps back to the raw parameters, added once
     float4* __restrict__ gsh = reinterpret_cast<float4*>(a.g_sh + 48 * (size_t)id);
 #pragma unroll
