@@ -27,6 +27,8 @@ def _gpu_params(rows, f16_sh=False):
     (400, 96, 80, (1.5, 0.5, 4.0), 5, None),
     (1000, 128, 128, (0.0, 0.0, 6.0), 3, (128, 1024)),       # stacked slabs: every slab's lists kept
     (3000, 112, 96, (1.0, -0.5, 5.0), 6, (64, 320, 1024)),
+    (600, 97, 61, (0.5, 0.2, 5.0), 8, None),                  # odd sizes: half-outside pixel pairs
+    (1200, 113, 77, (0.8, -0.3, 5.5), 9, (128, 1024)),
 ])
 def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed, slabs):
     import torch
@@ -66,8 +68,7 @@ def test_gradients_match_fp64_oracle(cuda, oracle, n, w, h, eye, seed, slabs):
 
 def test_train_forward_equals_plain_forward(cuda, oracle):
     """With binary16-representable SH the differentiable forward draws the plain forward's frame: to
-    float rounding at a floor of 2^-24, and within the floor at the default 1e-4 (the plain raster stops
-    per warp, the differentiable one per pixel)."""
+    float rounding at a floor of 2^-24, and within the floor at the default 1e-4."""
     import torch
     from vkgs_gb300 import Renderer, parse_ply, train
 
@@ -86,6 +87,36 @@ def test_train_forward_equals_plain_forward(cuda, oracle):
         rt.set_transmittance_floor(t_floor)
         img = train.render(_gpu_params(rows_f16), cam, rt)
         assert float((img.detach() - plain).abs().max()) <= tol, t_floor
+
+
+def test_lean_differentiable_path_equals_default(cuda, oracle):
+    """A lean context (gs_context_set_lean: the training raster with two pixels per thread on every slab)
+    draws the same image bit for bit and the same gradients (to float summation order) as a default one
+    (two pixels per thread on the nearest slab only), at an odd width with two slabs."""
+    import torch
+    from vkgs_gb300 import Renderer, train
+
+    n, w, h = 3000, 143, 87
+    rows = syn.splat_rows(n, 10)
+    c = scenes.camera(oracle, (0.6, -0.4, 5.0), width=w, height=h)
+    cam = scenes.product_camera(c)
+    weights = torch.tensor(np.random.default_rng(10).standard_normal((h, w, 4)), dtype=torch.float32,
+                           device="cuda")
+    out = []
+    for lean in (False, True):
+        r = Renderer(n, w, h)
+        r.set_slabs((128, 1024))
+        r.set_train_slab_min(0)
+        r.set_lean(lean)
+        params = _gpu_params(rows)
+        img = train.render(params, cam, r)
+        (img * weights).sum().backward()
+        out.append((img.detach().cpu().numpy(), {k: params[k].grad.double().cpu() for k in train.NAMES}))
+    (img_a, g_a), (img_b, g_b) = out
+    np.testing.assert_array_equal(img_a, img_b)
+    for name in train.NAMES:
+        rel = float((g_a[name] - g_b[name]).norm() / max(float(g_a[name].norm()), 1e-30))
+        assert rel <= 1e-5, (name, rel)
 
 
 def test_train_rejects_bad_shapes(cuda):
