@@ -398,10 +398,14 @@ constexpr u32 kPairBatch = 4;  // pairs per lane and step of the emission
 // returns the number of pairs.  The splats' row spans are listed
 // in shared memory (span = one tile row of one splat) with an exclusive prefix of their widths, so a
 // lane finds the span of pair j by binary search and no lane expands a footprint serially: a splat
-// that covers thousands of tiles costs the whole warp as much as that many small splats.
-// s_span: 2 * (kSpanBuf + 1) words of this warp's shared memory.  Whole warp.
+// that covers thousands of tiles costs the whole warp as much as that many small splats.  The rows are
+// clipped spread over the lanes too: each lane lists its splat's rows (owner lane, tile row), and the
+// lanes clip the listed rows in turn from the quads kept in shared memory, so a warp takes about
+// (its rows / 32) clip steps instead of the row count of its largest splat.
+// s_span: 2 * (kSpanBuf + 1) words, s_quad: 12 x 32 floats of this warp's shared memory.  Whole warp.
 template <class F>
-__device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const TargetGeom& g, u32* s_span, F&& fn) {
+__device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const TargetGeom& g, u32* s_span,
+                                             float (*s_quad)[32], F&& fn) {
   u32* s_tile = s_span;                // tile id of the span's first column << 5 | owner lane
   u32* s_pfx = s_span + kSpanBuf + 1;  // exclusive prefix of the span widths, [m] = total
   const u32 lane = threadIdx.x & 31u;
@@ -414,18 +418,38 @@ __device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const 
   }
   const u32 rfirst = incl - nrows;
   const u32 total_rows = __shfl_sync(0xffffffffu, incl, 31);
+  if (nrows) {  // the quad, for the lanes that clip this splat's rows
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      s_quad[k][lane] = f.vx[k];
+      s_quad[4 + k][lane] = f.vy[k];
+      s_quad[8 + k][lane] = f.dxdy[k];
+    }
+  }
   u32 done = 0;  // pairs of earlier windows
   for (u32 rw0 = 0; rw0 < total_rows; rw0 += kSpanBuf) {
+    __syncwarp();
+    // list this window's rows (owner lane, tile row), then clip them spread over the lanes
     const u32 i0 = max(rw0, rfirst), i1 = min(rfirst + nrows, rw0 + kSpanBuf);
-    for (u32 i = i0; i < i1; ++i) {
-      const int ty = f.ty0 + (int)(i - rfirst);
-      int tx0, tx1;
-      footprint_cols(f, g, ty, tx0, tx1);
-      s_tile[i - rw0] = ((u32)(ty * (int)g.tiles_x + max(tx0, 0)) << 5) | lane;
-      s_pfx[i - rw0] = (u32)max(0, tx1 - tx0 + 1);  // width for now
-    }
+    for (u32 i = i0; i < i1; ++i) s_tile[i - rw0] = ((u32)(f.ty0 + (int)(i - rfirst)) << 5) | lane;
     __syncwarp();
     const u32 m = min(kSpanBuf, total_rows - rw0);
+    for (u32 e = lane; e < m; e += 32) {
+      const u32 v = s_tile[e], owner = v & 31u;
+      const int ty = (int)(v >> 5);
+      Footprint fo;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        fo.vx[k] = s_quad[k][owner];
+        fo.vy[k] = s_quad[4 + k][owner];
+        fo.dxdy[k] = s_quad[8 + k][owner];
+      }
+      int tx0, tx1;
+      footprint_cols(fo, g, ty, tx0, tx1);
+      s_tile[e] = ((u32)(ty * (int)g.tiles_x + max(tx0, 0)) << 5) | owner;
+      s_pfx[e] = (u32)max(0, tx1 - tx0 + 1);  // width for now
+    }
+    __syncwarp();
     // exclusive scan of the m widths in place: each lane owns kSpanBuf/32 consecutive entries
     constexpr u32 kPer = kSpanBuf / 32;
     u32 w[kPer], s = 0;
@@ -485,6 +509,7 @@ __device__ __forceinline__ u32 for_each_pair(const Footprint& f, bool ok, const 
 //    for_each_pair and appends each open pair's sorted position to its tile's segment.
 __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
   __shared__ u32 s_spans[kEmitWarps][2 * (kSpanBuf + 1)];
+  __shared__ float s_quads[kEmitWarps][12][32];
   const u32 warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const SlabBounds sb = slab(a);
   const TargetGeom g = target_geom(a);
@@ -496,7 +521,7 @@ __global__ __launch_bounds__(kEmitThreads) void k_bin_emit(const BinArgs a) {
     Footprint f;
     bool ok = false;
     if (c > 0) ok = footprint(a.record, __ldg(a.index + r), g, f);
-    for_each_pair(f, ok, g, s_spans[warp], [&](const bool* has, const u32* tile, const u32* owner) {
+    for_each_pair(f, ok, g, s_spans[warp], s_quads[warp], [&](const bool* has, const u32* tile, const u32* owner) {
       u32 pos[kPairBatch];
 #pragma unroll
       for (u32 q = 0; q < kPairBatch; ++q) {  // all slots reserved first: the atomics overlap
