@@ -197,7 +197,7 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
 // memory holds the values the packed operations take twice, side by side.
 constexpr int kPairThreads = kTile * kTile / 2;
 constexpr int kPairWarps = kPairThreads / 32;  // 4 blocks of 64 pixels
-constexpr int kPairBatch = 256;                // records per batch, two per thread
+constexpr int kPairBatch = 128;                // records per batch, one per thread (256: ~1 % fewer frames/s in flight)
 constexpr int kPairLoads = kPairBatch / kPairThreads;
 constexpr int kPairWords = kPairBatch / 32;
 
