@@ -188,7 +188,7 @@ __global__ __launch_bounds__(kRasterThreads, 5) void k_raster(const RasterArgs a
   }
 }
 
-// The plain and the counting forward with two horizontally adjacent pixels per thread: 128 threads
+// The plain, counting and differentiable forwards with two horizontally adjacent pixels per thread: 128 threads
 // per tile, each warp owning an 8x8 block (4 pixel pairs x 8 rows).  A record's shared-memory loads,
 // the walk over the block's record bits and the vertical offset serve both pixels of a thread; each
 // pixel's coverage test keeps the explicitly rounded scalar operations above (the pair's dx is one
@@ -200,12 +200,13 @@ constexpr int kPairWarps = kPairThreads / 32;  // 4 blocks of 64 pixels
 constexpr int kPairBatch = 128;                // records per batch, one per thread (256: ~1 % fewer frames/s in flight)
 constexpr int kPairLoads = kPairBatch / kPairThreads;
 constexpr int kPairWords = kPairBatch / 32;
+static_assert(kPairLoads >= 1 && kPairBatch % kPairThreads == 0, "every thread loads whole records");
 
 constexpr int kPairBW = 8, kPairBH = 8, kPairBX = kTile / kPairBW;  // 8x8 blocks, 2 x 2 per tile
 static_assert(kPairWarps * kPairBW * kPairBH == kTile * kTile && kPairBW * kPairBH == 64, "pair blocks");
 
-template <bool DEPTH, bool COUNT, bool TRAIN>
 // 9 CTAs per SM (56 registers): 921-922 vs 918 frames/s with frames in flight against 8 (64 registers)
+template <bool DEPTH, bool COUNT, bool TRAIN>
 __global__ __launch_bounds__(kPairThreads, 9) void k_raster_pairs(const RasterArgs a) {
   __shared__ float4 s_a[kPairBatch];  // (-cx, -cx, -cy, m00)
   __shared__ float4 s_b[kPairBatch];  // (m01, m10, m11, z)
